@@ -1,0 +1,222 @@
+/* ostaple_gb300.h -- C ABI of the GB300 (sm_103a) staggered-fermion hot path.
+ *
+ * Drop-in for the reference's OpenACC hot path: the functions below carry the
+ * reference's own names, argument order, argument meaning and return codes,
+ * so that the reference's unmodified C host code can link against this
+ * library instead of fermion_matrix.o, fermionic_utilities.o, inverter_*.o,
+ * stouting.o and fermion_force*.o.  Each declaration cites the reference
+ * declaration it replaces (paths relative to the reference source tree).
+ *
+ * Differences a host program must know about:
+ *   - The lattice size is given at run time by ostaple_init() instead of the
+ *     compile-time LOC_N0..3 macros (geometry_multidev.h:78-85).  Buffers keep
+ *     the reference's layouts, sized by that lattice.
+ *   - OpenACC `enter data create` / `update device|host` / `exit data`
+ *     become ostaple_enter_data / ostaple_update_device / ostaple_update_host
+ *     / ostaple_exit_data.  A pointer passed to a hot-path function must
+ *     either be registered that way (the host address is then translated to
+ *     its device mirror, like OpenACC's `present`) or be a device pointer.
+ *   - Work is queued on one library stream (ostaple_set_stream() to share a
+ *     caller stream).  Functions that return a scalar synchronise;
+ *     ostaple_update_host synchronises; ostaple_synchronize() waits for all.
+ *   - Errors are recorded (ostaple_get_error / ostaple_last_error); functions
+ *     whose reference signature returns a status return the reference's
+ *     INVERTER_SUCCESS / INVERTER_FAILURE.
+ */
+#ifndef OSTAPLE_GB300_H_
+#define OSTAPLE_GB300_H_
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- reference types --------------------------------------------------- */
+/* SoA field types are opaque here: their size follows the run-time lattice.
+ * The struct tags match the reference's (struct_c_def.h:16-60), so a host
+ * that also includes the reference's struct_c_def.h sees compatible types. */
+typedef struct vec3_soa_t vec3_soa;       /* c0,c1,c2 [sizeh] double complex */
+typedef struct su3_soa_t su3_soa;         /* r0,r1,r2 vec3_soa               */
+typedef struct double_soa_t double_soa;   /* d[sizeh]                        */
+typedef struct tamat_soa_t tamat_soa;     /* c01,c02,c12 complex; ic00,ic11  */
+typedef struct thmat_soa_t thmat_soa;     /* c01,c02,c12 complex; rc00,rc11  */
+typedef struct vec3_soa_f_t vec3_soa_f;   /* float twins (generated sp_ types) */
+typedef struct su3_soa_f_t su3_soa_f;
+typedef struct float_soa_t float_soa;
+
+#define INVERTER_SUCCESS 1                /* inverter_full.h:12 */
+#define INVERTER_FAILURE 0                /* inverter_full.h:13 */
+#define MAX_APPROX_ORDER 25               /* rationalapprox.h:8 */
+#define CONVERGENCE_CRITICAL 1            /* inverter_wrappers.h:11 */
+#define CONVERGENCE_NONCRITICAL 0         /* inverter_wrappers.h:12 */
+
+/* Plain structs whose layout must equal the reference's.  Define
+ * OSTAPLE_HAVE_REFERENCE_TYPES when the reference's own headers are included
+ * in the same translation unit. */
+#ifndef OSTAPLE_HAVE_REFERENCE_TYPES
+typedef struct RationalApprox_t {          /* rationalapprox.h:15-26 */
+  int exponent_num;
+  int exponent_den;
+  int approx_order;
+  double lambda_min;
+  double lambda_max;
+  int gmp_remez_precision;
+  double error;
+  double RA_a0;
+  double RA_a[MAX_APPROX_ORDER];
+  double RA_b[MAX_APPROX_ORDER];
+} RationalApprox;
+
+typedef struct ferm_param_t {             /* Include/fermion_parameters.h:9-41 */
+  double ferm_mass;
+  int degeneracy;
+  int number_of_ps;
+  char name[30];
+  double ferm_charge;
+  double ferm_im_chem_pot;
+  int index_of_the_first_ps;
+  int index_of_the_first_shift;
+  double_soa *phases;
+  double_soa *mag_re;
+  double_soa *mag_im;
+  int printed_bf_dbg_info;
+  float_soa *phases_f;
+  RationalApprox approx_fi_mother;
+  RationalApprox approx_md_mother;
+  RationalApprox approx_li_mother;
+  RationalApprox approx_fi;
+  RationalApprox approx_md;
+  RationalApprox approx_li;
+} ferm_param;
+
+typedef struct inv_tricks_t {             /* Include/inverter_tricks.h:4-11 */
+  int singlePInvAccelMultiInv;
+  int useMixedPrecision;
+  double mixedPrecisionDelta;
+  int restartingEvery;
+} inv_tricks;
+
+typedef struct inverter_package_t {       /* OpenAcc/inverter_package.h:13-31 */
+  const su3_soa *u;
+  const su3_soa_f *u_f;
+  vec3_soa *ferm_shift_temp;
+  vec3_soa_f *ferm_shift_temp_f;
+  int nshifts;
+  vec3_soa *loc_r;
+  vec3_soa *loc_h;
+  vec3_soa *loc_s;
+  vec3_soa *loc_p;
+  vec3_soa_f *loc_r_f;
+  vec3_soa_f *loc_h_f;
+  vec3_soa_f *loc_s_f;
+  vec3_soa_f *loc_p_f;
+  vec3_soa_f *out_f;
+} inverter_package;
+#endif
+
+/* Inverter switches read by the dispatch wrappers.  The reference host
+ * defines this global (Include/inverter_tricks.c); the library carries a
+ * weak default {0, 0, 0.1, 10000} that a host definition overrides. */
+extern inv_tricks inverter_tricks;
+
+/* ---- runtime (replaces compile-time geometry and OpenACC data clauses) -- */
+/* set_geom_glv (geometry.c:103-180) + select_init_acc_device (deviceinit.c:14-36).
+ * Extents must be even.  Returns 0 on success. */
+int ostaple_init(int n0, int n1, int n2, int n3);
+int ostaple_finalize(void);
+int ostaple_sizeh(void);
+int ostaple_set_stream(void *cuda_stream);
+int ostaple_synchronize(void);
+int ostaple_get_error(void);
+const char *ostaple_last_error(void);
+void ostaple_clear_error(void);
+/* `#pragma acc enter data create(p[0:bytes])` (alloc_vars.c:94-284) */
+int ostaple_enter_data(const void *host, size_t bytes);
+/* `#pragma acc exit data delete(p)` */
+int ostaple_exit_data(const void *host);
+/* `#pragma acc update device(p[0:bytes])` / `update host(...)` */
+int ostaple_update_device(const void *host, size_t bytes);
+int ostaple_update_host(void *host, size_t bytes);
+/* acc_deviceptr(): device mirror of a registered host address, or NULL */
+void *ostaple_deviceptr(const void *host);
+
+/* Measured FMA throughput of this device in TFLOP/s (fp64 != 0: FP64, else
+ * FP32); the ceiling of the compute-bound FP64 kernels.  No reference
+ * counterpart. */
+int ostaple_probe_fma_tflops(int fp64, double *tflops);
+
+/* ---- staggered Dirac operator (fermion_matrix.h:20-39) ----------------- */
+/* out(even) = 1/2 sum_mu [ e^{i th} U_mu(x) in(x+mu) - e^{-i th} U_mu(x-mu)^+ in(x-mu) ] */
+void acc_Deo(const su3_soa *u, vec3_soa *out, const vec3_soa *in, const double_soa *backfield);
+/* the same with even and odd exchanged */
+void acc_Doe(const su3_soa *u, vec3_soa *out, const vec3_soa *in, const double_soa *backfield);
+/* without halo exchange (identical on one GPU) (fermion_matrix.h:29-39) */
+void acc_Deo_unsafe(const su3_soa *u, vec3_soa *out, const vec3_soa *in, const double_soa *backfield);
+void acc_Doe_unsafe(const su3_soa *u, vec3_soa *out, const vec3_soa *in, const double_soa *backfield);
+
+/* out = m^2 in - D_eo D_oe in, temp1 receives D_oe in (fermion_matrix.h:95-99) */
+void fermion_matrix_multiplication(const su3_soa *u, vec3_soa *out, const vec3_soa *in,
+                                   vec3_soa *temp1, ferm_param *pars);
+/* out = (m^2 + shift) in - D_eo D_oe in (fermion_matrix.h:101-106) */
+void fermion_matrix_multiplication_shifted(const su3_soa *u, vec3_soa *out, const vec3_soa *in,
+                                           vec3_soa *temp1, ferm_param *pars, double shift);
+
+/* ---- fermion BLAS and global reductions (fermionic_utilities.h:38-123) - */
+/* sum_x conj(a).b (fermionic_utilities.h:38-39).  The reference returns a
+ * C99 `double complex`; a struct of two doubles is returned in the same
+ * registers on x86-64 (SysV) and AArch64 (AAPCS64), so the symbol is
+ * call-compatible with the reference's declaration. */
+#ifndef OSTAPLE_HAVE_REFERENCE_TYPES
+typedef struct ostaple_dcomplex_t { double re, im; } ostaple_dcomplex;
+ostaple_dcomplex scal_prod_global(const vec3_soa *in_vect1, const vec3_soa *in_vect2);
+#endif
+/* the same, writing {re, im} to re_im (for FFI callers without complex types) */
+void scal_prod_global_ri(const vec3_soa *in_vect1, const vec3_soa *in_vect2, double *re_im);
+double real_scal_prod_global(const vec3_soa *in_vect1, const vec3_soa *in_vect2); /* :40 */
+double l2norm2_global(const vec3_soa *in_vect1);                                  /* :42 */
+void combine_in1xfactor_plus_in2(const vec3_soa *in_vect1, const double factor,
+                                 const vec3_soa *in_vect2, vec3_soa *out);        /* :48 */
+void multiply_fermion_x_doublefactor(vec3_soa *in1, const double factor);         /* :55 */
+void combine_add_factor_x_in2_to_in1(vec3_soa *in1, const vec3_soa *in2, double factor); /* :59 */
+void combine_in1xferm_mass2_minus_in2_minus_in3(const vec3_soa *in_vect1, double ferm_mass,
+                                                const vec3_soa *in_vect2, const vec3_soa *in_vect3,
+                                                vec3_soa *out);                   /* :67 */
+void combine_inside_loop(vec3_soa *vect_out, vec3_soa *vect_r, const vec3_soa *vect_s,
+                         const vec3_soa *vect_p, const double omega);             /* :75 */
+void combine_in1xferm_mass_minus_in2(const vec3_soa *in_vect1, double ferm_mass2,
+                                     vec3_soa *in_vect2);                         /* :81 */
+void combine_in1_minus_in2(const vec3_soa *in_vect1, const vec3_soa *in_vect2, vec3_soa *out); /* :86 */
+void assign_in_to_out(const vec3_soa *in_vect1, vec3_soa *out);                   /* :90 */
+void set_vec3_soa_to_zero(vec3_soa *fermion);                                     /* :94 */
+void multiple_combine_in1_minus_in2x_factor_back_into_in1(vec3_soa *out, const vec3_soa *in,
+                                                          const int maxiter, const int *flag,
+                                                          const double *omegas);  /* :95 */
+void multiple1_combine_in1_x_fact1_plus_in2_x_fact2_back_into_in1(
+    vec3_soa *in1, int maxiter, const int *flag, const double *gammas, const vec3_soa *in2,
+    const double *zeta_iii);                                                      /* :100 */
+void combine_in1_x_fact1_minus_in2_back_into_in2(const vec3_soa *in1, double fact1,
+                                                 vec3_soa *in2);                  /* :106 */
+void combine_in1_minus_in2_allxfact(const vec3_soa *in1, const vec3_soa *in2, double fact,
+                                    vec3_soa *out);                               /* :109 */
+
+/* ---- solvers ------------------------------------------------------------ */
+/* CG on (M^+M + shift) x = in, restarted every inverter_tricks.restartingEvery
+ * iterations (inverter_full.h:20-31). */
+int ker_invert_openacc(const su3_soa *u, ferm_param *pars, vec3_soa *solution, const vec3_soa *in,
+                       double res, vec3_soa *loc_r, vec3_soa *loc_h, vec3_soa *loc_s,
+                       vec3_soa *loc_p, const int max_cg, double shift, int *cg_return);
+/* CG-M for all shifts of approx (inverter_multishift_full.h:15-27) */
+int multishift_invert(const su3_soa *u, ferm_param *pars, RationalApprox *approx, vec3_soa *out,
+                      const vec3_soa *in, double residuo, vec3_soa *loc_r, vec3_soa *loc_h,
+                      vec3_soa *loc_s, vec3_soa *loc_p, vec3_soa *shiftferm, const int max_cg,
+                      int *cg_return);
+/* out = a0 in + sum_i a_i in_shifted[i] (inverter_multishift_full.h:30-33) */
+void recombine_shifted_vec3_to_vec3(const vec3_soa *in_shifted, const vec3_soa *in, vec3_soa *out,
+                                    const RationalApprox *approx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* OSTAPLE_GB300_H_ */

@@ -1,0 +1,168 @@
+"""Python mirror of the reference's hot-path interface.
+
+Functions carry the reference's names and argument order
+(fermion_matrix.h, fermionic_utilities.h, inverter_full.h,
+inverter_multishift_full.h) and take numpy arrays in the reference's SoA
+layouts.  Host arrays are made present on the device with
+:meth:`Lattice.present` (the OpenACC ``enter data`` + ``update device``
+pair) and read back with :meth:`Lattice.update_host`; every compute call goes
+to the CUDA library.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Sequence
+
+import numpy as np
+
+from .native import FermParam, RationalApprox, check, inverter_tricks, lib
+
+
+def ptr(a) -> int:
+    """Address of a numpy array or a CUDA tensor (``data_ptr``)."""
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data
+    if hasattr(a, "data_ptr"):
+        return a.data_ptr()
+    if isinstance(a, int):
+        return a
+    raise TypeError(f"cannot take the address of {type(a)}")
+
+
+class Lattice:
+    """Initialises the library for one lattice and tracks device mirrors."""
+
+    def __init__(self, dims: Sequence[int]):
+        self.dims = tuple(int(d) for d in dims)
+        self.L = lib()
+        rc = self.L.ostaple_init(*self.dims)
+        check(rc, "ostaple_init")
+        self.sizeh = self.L.ostaple_sizeh()
+        self._present: dict[int, int] = {}
+
+    def present(self, arr: np.ndarray, copy: bool = True) -> np.ndarray:
+        if not arr.flags["C_CONTIGUOUS"]:
+            raise ValueError("arrays must be C-contiguous")
+        p = arr.ctypes.data
+        if p not in self._present:
+            check(self.L.ostaple_enter_data(p, arr.nbytes), "enter_data")
+            self._present[p] = arr.nbytes
+        if copy:
+            check(self.L.ostaple_update_device(p, arr.nbytes), "update_device")
+        return arr
+
+    def update_device(self, arr: np.ndarray) -> None:
+        check(self.L.ostaple_update_device(arr.ctypes.data, arr.nbytes), "update_device")
+
+    def update_host(self, arr: np.ndarray) -> np.ndarray:
+        check(self.L.ostaple_update_host(arr.ctypes.data, arr.nbytes), "update_host")
+        return arr
+
+    def release(self, arr: np.ndarray) -> None:
+        p = arr.ctypes.data
+        if p in self._present:
+            self.L.ostaple_exit_data(p)
+            del self._present[p]
+
+    def release_all(self) -> None:
+        for p in list(self._present):
+            self.L.ostaple_exit_data(p)
+        self._present.clear()
+
+    def sync(self) -> None:
+        check(self.L.ostaple_synchronize(), "synchronize")
+
+    # --- field constructors in the reference layouts ---
+    def vec3(self, n: int | None = None) -> np.ndarray:
+        shape = (3, self.sizeh) if n is None else (n, 3, self.sizeh)
+        return np.zeros(shape, dtype=np.complex128)
+
+    def close(self) -> None:
+        self.release_all()
+        self.L.ostaple_finalize()
+
+
+def make_ferm_param(mass: float, phases: np.ndarray | int) -> FermParam:
+    fp = FermParam()
+    fp.ferm_mass = float(mass)
+    fp.degeneracy = 1
+    fp.number_of_ps = 1
+    fp.phases = ptr(phases)
+    return fp
+
+
+def make_approx(a0: float, a: Sequence[float], b: Sequence[float]) -> RationalApprox:
+    ra = RationalApprox()
+    ra.approx_order = len(a)
+    ra.RA_a0 = float(a0)
+    for i, (ai, bi) in enumerate(zip(a, b)):
+        ra.RA_a[i] = float(ai)
+        ra.RA_b[i] = float(bi)
+    return ra
+
+
+# ---- reference-named calls ----
+def acc_Deo(u, out, inp, backfield) -> None:
+    lib().acc_Deo(ptr(u), ptr(out), ptr(inp), ptr(backfield))
+    check(0, "acc_Deo")
+
+
+def acc_Doe(u, out, inp, backfield) -> None:
+    lib().acc_Doe(ptr(u), ptr(out), ptr(inp), ptr(backfield))
+    check(0, "acc_Doe")
+
+
+def fermion_matrix_multiplication_shifted(u, out, inp, temp1, pars: FermParam, shift: float) -> None:
+    lib().fermion_matrix_multiplication_shifted(ptr(u), ptr(out), ptr(inp), ptr(temp1), C.byref(pars), shift)
+    check(0, "fermion_matrix_multiplication_shifted")
+
+
+def fermion_matrix_multiplication(u, out, inp, temp1, pars: FermParam) -> None:
+    lib().fermion_matrix_multiplication(ptr(u), ptr(out), ptr(inp), ptr(temp1), C.byref(pars))
+    check(0, "fermion_matrix_multiplication")
+
+
+def l2norm2_global(v) -> float:
+    r = lib().l2norm2_global(ptr(v))
+    check(0, "l2norm2_global")
+    return r
+
+
+def real_scal_prod_global(a, b) -> float:
+    r = lib().real_scal_prod_global(ptr(a), ptr(b))
+    check(0, "real_scal_prod_global")
+    return r
+
+
+def scal_prod_global(a, b) -> complex:
+    out = (C.c_double * 2)()
+    lib().scal_prod_global_ri(ptr(a), ptr(b), out)
+    check(0, "scal_prod_global")
+    return complex(out[0], out[1])
+
+
+def ker_invert_openacc(u, pars: FermParam, solution, inp, res: float, loc_r, loc_h, loc_s, loc_p, max_cg: int,
+                       shift: float) -> tuple[int, int]:
+    cg = C.c_int(0)
+    st = lib().ker_invert_openacc(ptr(u), C.byref(pars), ptr(solution), ptr(inp), res, ptr(loc_r), ptr(loc_h),
+                                  ptr(loc_s), ptr(loc_p), max_cg, shift, C.byref(cg))
+    check(0, "ker_invert_openacc")
+    return st, cg.value
+
+
+def multishift_invert(u, pars: FermParam, approx: RationalApprox, out, inp, residuo: float, loc_r, loc_h, loc_s,
+                      loc_p, shiftferm, max_cg: int) -> tuple[int, int]:
+    cg = C.c_int(0)
+    st = lib().multishift_invert(ptr(u), C.byref(pars), C.byref(approx), ptr(out), ptr(inp), residuo, ptr(loc_r),
+                                 ptr(loc_h), ptr(loc_s), ptr(loc_p), ptr(shiftferm), max_cg, C.byref(cg))
+    check(0, "multishift_invert")
+    return st, cg.value
+
+
+def recombine_shifted_vec3_to_vec3(in_shifted, inp, out, approx: RationalApprox) -> None:
+    lib().recombine_shifted_vec3_to_vec3(ptr(in_shifted), ptr(inp), ptr(out), C.byref(approx))
+    check(0, "recombine_shifted_vec3_to_vec3")
+
+
+def set_restarting_every(n: int) -> None:
+    inverter_tricks().restartingEvery = int(n)

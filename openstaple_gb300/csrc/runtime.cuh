@@ -1,0 +1,69 @@
+// runtime.cuh -- library-internal runtime: geometry, stream, device
+// residency registry, error state, and a growable device workspace.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+#include "common.cuh"
+
+namespace ost {
+
+struct Runtime {
+  bool initialized = false;
+  int device = 0;
+  int num_sms = 0;
+  Geom g{};
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+};
+
+Runtime& rt();
+
+// Error state: the reference's void entry points report through printf; this
+// library records the first failure and returns failure codes where the
+// reference signature has one.
+void set_error(int code, const char* fmt, ...);
+int error_code();
+const char* error_message();
+void clear_error();
+
+#define OST_CUDA(call)                                                       \
+  do {                                                                       \
+    cudaError_t e_ = (call);                                                 \
+    if (e_ != cudaSuccess) {                                                 \
+      ::ost::set_error(int(e_), "%s:%d %s -> %s", __FILE__, __LINE__, #call, \
+                       cudaGetErrorString(e_));                              \
+    }                                                                        \
+  } while (0)
+
+#define OST_LAUNCH_CHECK() OST_CUDA(cudaGetLastError())
+
+bool require_init(const char* who);
+
+// Host pointer -> device mirror (the OpenACC `present` table).  A pointer that
+// is not registered but already addresses device memory is used as is.
+// Returns nullptr (and records an error) if the pointer is neither.
+void* resolve(const void* p, const char* what);
+template <typename T> T* dev(const T* p, const char* what) {
+  return static_cast<T*>(resolve(static_cast<const void*>(p), what));
+}
+
+// Growable named device workspace; buffers persist until finalize.
+void* workspace(int slot, size_t bytes);
+enum WorkspaceSlot {
+  WS_REDUCE = 0,   // block partial sums
+  WS_SCALARS,      // device-resident solver scalars
+  WS_VEC0, WS_VEC1, WS_VEC2, WS_VEC3, WS_VEC4, WS_VEC5,
+  WS_LINKS_F32,    // FP32 copy of links for the mixed/batched solvers
+  WS_SIGNS,        // per-link staggered sign bytes
+  WS_MULTI,        // multi-shift / multi-RHS vectors
+  WS_MULTI2,
+  WS_FORCE0, WS_FORCE1, WS_FORCE2, WS_FORCE3,
+  WS_NET,          // learned preconditioner weights and activations
+  WS_NET2,
+  WS_NSLOTS
+};
+
+inline int blocks_for(long n, int threads) { return int((n + threads - 1) / threads); }
+
+}  // namespace ost

@@ -1,0 +1,160 @@
+"""ctypes binding of the in-tree CUDA library ``libostaple_gb300.so``.
+
+The library is the product: every hot-path call below goes to a hand-written
+sm_103a kernel.  There is no fallback: if the shared library is missing or
+cannot be loaded, :func:`lib` raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "libostaple_gb300.so"
+MAX_APPROX_ORDER = 25  # rationalapprox.h:8
+INVERTER_SUCCESS = 1
+INVERTER_FAILURE = 0
+
+
+class RationalApprox(C.Structure):
+    """Layout of the reference's RationalApprox (rationalapprox.h:15-26)."""
+    _fields_ = [
+        ("exponent_num", C.c_int),
+        ("exponent_den", C.c_int),
+        ("approx_order", C.c_int),
+        ("lambda_min", C.c_double),
+        ("lambda_max", C.c_double),
+        ("gmp_remez_precision", C.c_int),
+        ("error", C.c_double),
+        ("RA_a0", C.c_double),
+        ("RA_a", C.c_double * MAX_APPROX_ORDER),
+        ("RA_b", C.c_double * MAX_APPROX_ORDER),
+    ]
+
+
+class FermParam(C.Structure):
+    """Layout of the reference's ferm_param (Include/fermion_parameters.h:9-41)."""
+    _fields_ = [
+        ("ferm_mass", C.c_double),
+        ("degeneracy", C.c_int),
+        ("number_of_ps", C.c_int),
+        ("name", C.c_char * 30),
+        ("ferm_charge", C.c_double),
+        ("ferm_im_chem_pot", C.c_double),
+        ("index_of_the_first_ps", C.c_int),
+        ("index_of_the_first_shift", C.c_int),
+        ("phases", C.c_void_p),
+        ("mag_re", C.c_void_p),
+        ("mag_im", C.c_void_p),
+        ("printed_bf_dbg_info", C.c_int),
+        ("phases_f", C.c_void_p),
+        ("approx_fi_mother", RationalApprox),
+        ("approx_md_mother", RationalApprox),
+        ("approx_li_mother", RationalApprox),
+        ("approx_fi", RationalApprox),
+        ("approx_md", RationalApprox),
+        ("approx_li", RationalApprox),
+    ]
+
+
+class InvTricks(C.Structure):
+    """Layout of the reference's inv_tricks (Include/inverter_tricks.h:4-11)."""
+    _fields_ = [
+        ("singlePInvAccelMultiInv", C.c_int),
+        ("useMixedPrecision", C.c_int),
+        ("mixedPrecisionDelta", C.c_double),
+        ("restartingEvery", C.c_int),
+    ]
+
+
+class InverterPackage(C.Structure):
+    """Layout of the reference's inverter_package (OpenAcc/inverter_package.h:13-31)."""
+    _fields_ = [
+        ("u", C.c_void_p), ("u_f", C.c_void_p),
+        ("ferm_shift_temp", C.c_void_p), ("ferm_shift_temp_f", C.c_void_p),
+        ("nshifts", C.c_int),
+        ("loc_r", C.c_void_p), ("loc_h", C.c_void_p), ("loc_s", C.c_void_p), ("loc_p", C.c_void_p),
+        ("loc_r_f", C.c_void_p), ("loc_h_f", C.c_void_p), ("loc_s_f", C.c_void_p), ("loc_p_f", C.c_void_p),
+        ("out_f", C.c_void_p),
+    ]
+
+
+_P = C.c_void_p
+_D = C.c_double
+_I = C.c_int
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "ostaple_init": (_I, [_I, _I, _I, _I]),
+    "ostaple_finalize": (_I, []),
+    "ostaple_sizeh": (_I, []),
+    "ostaple_set_stream": (_I, [_P]),
+    "ostaple_synchronize": (_I, []),
+    "ostaple_get_error": (_I, []),
+    "ostaple_last_error": (C.c_char_p, []),
+    "ostaple_clear_error": (None, []),
+    "ostaple_enter_data": (_I, [_P, C.c_size_t]),
+    "ostaple_exit_data": (_I, [_P]),
+    "ostaple_update_device": (_I, [_P, C.c_size_t]),
+    "ostaple_update_host": (_I, [_P, C.c_size_t]),
+    "ostaple_deviceptr": (_P, [_P]),
+    "ostaple_probe_fma_tflops": (_I, [_I, C.POINTER(_D)]),
+    "acc_Deo": (None, [_P, _P, _P, _P]),
+    "acc_Doe": (None, [_P, _P, _P, _P]),
+    "acc_Deo_unsafe": (None, [_P, _P, _P, _P]),
+    "acc_Doe_unsafe": (None, [_P, _P, _P, _P]),
+    "fermion_matrix_multiplication": (None, [_P, _P, _P, _P, C.POINTER(FermParam)]),
+    "fermion_matrix_multiplication_shifted": (None, [_P, _P, _P, _P, C.POINTER(FermParam), _D]),
+    "scal_prod_global_ri": (None, [_P, _P, C.POINTER(_D)]),
+    "real_scal_prod_global": (_D, [_P, _P]),
+    "l2norm2_global": (_D, [_P]),
+    "combine_in1xfactor_plus_in2": (None, [_P, _D, _P, _P]),
+    "multiply_fermion_x_doublefactor": (None, [_P, _D]),
+    "combine_add_factor_x_in2_to_in1": (None, [_P, _P, _D]),
+    "combine_in1xferm_mass2_minus_in2_minus_in3": (None, [_P, _D, _P, _P, _P]),
+    "combine_inside_loop": (None, [_P, _P, _P, _P, _D]),
+    "combine_in1xferm_mass_minus_in2": (None, [_P, _D, _P]),
+    "combine_in1_minus_in2": (None, [_P, _P, _P]),
+    "assign_in_to_out": (None, [_P, _P]),
+    "set_vec3_soa_to_zero": (None, [_P]),
+    "multiple_combine_in1_minus_in2x_factor_back_into_in1": (None, [_P, _P, _I, C.POINTER(_I), C.POINTER(_D)]),
+    "multiple1_combine_in1_x_fact1_plus_in2_x_fact2_back_into_in1":
+        (None, [_P, _I, C.POINTER(_I), C.POINTER(_D), _P, C.POINTER(_D)]),
+    "combine_in1_x_fact1_minus_in2_back_into_in2": (None, [_P, _D, _P]),
+    "combine_in1_minus_in2_allxfact": (None, [_P, _P, _D, _P]),
+    "ker_invert_openacc": (_I, [_P, C.POINTER(FermParam), _P, _P, _D, _P, _P, _P, _P, _I, _D, C.POINTER(_I)]),
+    "multishift_invert": (_I, [_P, C.POINTER(FermParam), C.POINTER(RationalApprox), _P, _P, _D, _P, _P, _P, _P,
+                               _P, _I, C.POINTER(_I)]),
+    "recombine_shifted_vec3_to_vec3": (None, [_P, _P, _P, C.POINTER(RationalApprox)]),
+}
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """Loads the CUDA library (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise RuntimeError(
+                f"{LIB_PATH} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`")
+        L = C.CDLL(str(LIB_PATH), mode=C.RTLD_GLOBAL)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def inverter_tricks() -> InvTricks:
+    """The library's `inverter_tricks` global (writable)."""
+    return InvTricks.in_dll(lib(), "inverter_tricks")
+
+
+def check(ret: int = 0, what: str = "") -> None:
+    L = lib()
+    code = L.ostaple_get_error()
+    if code != 0 or (isinstance(ret, int) and ret < 0):
+        msg = L.ostaple_last_error().decode()
+        L.ostaple_clear_error()
+        raise RuntimeError(f"ostaple error in {what}: {msg} (code {code}, ret {ret})")

@@ -1,0 +1,193 @@
+"""Test oracle (checker only): ctypes bindings of
+
+* ``oracle/liboracle.so`` -- the CPU restatement in ``ostaple_oracle.c``;
+* ``oracle/_ref/libref_<dims>.so`` -- the reference's own C sources compiled
+  per lattice size by ``Makefile.ref`` (present only where the reference
+  source tree was available at build time).
+
+Only the tests, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg
+use this package.  The product never imports it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ORACLE_LIB = HERE / "liboracle.so"
+REF_DIR = HERE / "_ref"
+
+_P, _D, _I = C.c_void_p, C.c_double, C.c_int
+
+
+def _p(a: np.ndarray) -> int:
+    assert a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data
+
+
+class Oracle:
+    """The CPU restatement (runtime geometry)."""
+
+    _sig = {
+        "orc_init": (_I, [_I, _I, _I, _I]),
+        "orc_sizeh": (_I, []),
+        "orc_set_threads": (None, [_I]),
+        "orc_calc_phases": (None, [_P, _D]),
+        "orc_Deo": (None, [_P, _P, _P, _P]),
+        "orc_Doe": (None, [_P, _P, _P, _P]),
+        "orc_mdagm": (None, [_P, _P, _P, _P, _P, _D]),
+        "orc_norm2": (_D, [_P]),
+        "orc_rdot": (_D, [_P, _P]),
+        "orc_cg": (_I, [_P, _P, _D, _P, _P, _D, _I, _D, _I, C.POINTER(_I)]),
+        "orc_cgm": (_I, [_P, _P, _D, _I, _P, _P, _P, _D, _I, C.POINTER(_I)]),
+        "orc_recombine": (None, [_P, _P, _P, _I, _D, _P]),
+    }
+
+    def __init__(self, dims, threads: int = 1):
+        if not ORACLE_LIB.exists():
+            raise RuntimeError(f"{ORACLE_LIB} missing: run __graft_entry__.build()")
+        self.L = C.CDLL(str(ORACLE_LIB))
+        for n, (r, a) in self._sig.items():
+            f = getattr(self.L, n)
+            f.restype = r
+            f.argtypes = a
+        self.dims = tuple(dims)
+        self.sizeh = self.L.orc_init(*self.dims)
+        self.L.orc_set_threads(threads)
+
+    def set_threads(self, n: int) -> None:
+        self.L.orc_set_threads(n)
+
+    def phases(self, im_chem_pot: float = 0.0) -> np.ndarray:
+        ph = np.zeros((8, self.sizeh))
+        self.L.orc_calc_phases(_p(ph), im_chem_pot)
+        return ph
+
+    def Deo(self, u, inp, ph):
+        out = np.zeros((3, self.sizeh), np.complex128)
+        self.L.orc_Deo(_p(u), _p(out), _p(inp), _p(ph))
+        return out
+
+    def Doe(self, u, inp, ph):
+        out = np.zeros((3, self.sizeh), np.complex128)
+        self.L.orc_Doe(_p(u), _p(out), _p(inp), _p(ph))
+        return out
+
+    def mdagm(self, u, inp, ph, m2):
+        out = np.zeros((3, self.sizeh), np.complex128)
+        tmp = np.zeros_like(out)
+        self.L.orc_mdagm(_p(u), _p(out), _p(inp), _p(tmp), _p(ph), m2)
+        return out
+
+    def norm2(self, a) -> float:
+        return self.L.orc_norm2(_p(a))
+
+    def cg(self, u, ph, mass, b, res, max_cg=10000, shift=0.0, restart=10000, x0=None):
+        x = np.zeros((3, self.sizeh), np.complex128) if x0 is None else x0.copy()
+        n = C.c_int(0)
+        st = self.L.orc_cg(_p(u), _p(ph), mass, _p(x), _p(b), res, max_cg, shift, restart, C.byref(n))
+        return st, n.value, x
+
+    def cgm(self, u, ph, mass, shifts, b, res, max_cg=10000):
+        shifts = np.ascontiguousarray(shifts, dtype=np.float64)
+        xs = np.zeros((len(shifts), 3, self.sizeh), np.complex128)
+        n = C.c_int(0)
+        st = self.L.orc_cgm(_p(u), _p(ph), mass, len(shifts), _p(shifts), _p(xs), _p(b), res, max_cg, C.byref(n))
+        return st, n.value, xs
+
+    def recombine(self, xs, b, a0, a):
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        out = np.zeros((3, self.sizeh), np.complex128)
+        self.L.orc_recombine(_p(xs), _p(b), _p(out), len(a), a0, _p(a))
+        return out
+
+
+def ref_available(dims) -> bool:
+    return (REF_DIR / ("libref_" + "x".join(map(str, dims)) + ".so")).exists()
+
+
+class Reference:
+    """The reference's own compiled C (one library per lattice size)."""
+
+    _sig = {
+        "ref_sizeh": (_I, []),
+        "ref_dims": (None, [_P]),
+        "ref_setup": (None, [_I]),
+        "ref_set_restart": (None, [_I]),
+        "ref_calc_phases": (None, [_P, _D, _D]),
+        "ref_Deo": (None, [_P, _P, _P, _P]),
+        "ref_Doe": (None, [_P, _P, _P, _P]),
+        "ref_mdagm_shifted": (None, [_P, _P, _P, _P, _P, _D, _D]),
+        "ref_l2norm2": (_D, [_P]),
+        "ref_real_scal_prod": (_D, [_P, _P]),
+        "ref_scal_prod": (None, [_P, _P, _P]),
+        "ref_cg": (_I, [_P, _P, _D, _P, _P, _D, _I, _D, C.POINTER(_I)]),
+        "ref_cgm": (_I, [_P, _P, _D, _I, _D, _P, _P, _P, _P, _D, _I, C.POINTER(_I)]),
+        "ref_recombine": (None, [_P, _P, _P, _I, _D, _P]),
+        "ref_stout_isotropic": (None, [_P, _P, _D]),
+        "ref_staples": (None, [_P, _P]),
+        "ref_rho_ta": (None, [_P, _P, _P, _D]),
+        "ref_force_outer_products": (None, [_P, _P, _P, _P, _D, _I, _P]),
+        "ref_backfield_times_force": (None, [_P, _P, _P]),
+        "ref_sigma_prime_to_sigma": (None, [_P, _P, _D]),
+        "ref_conf_times_force_ta": (None, [_P, _P, _P]),
+        "ref_set_tamat_zero": (None, [_P]),
+    }
+
+    def __init__(self, dims):
+        path = REF_DIR / ("libref_" + "x".join(map(str, dims)) + ".so")
+        if not path.exists():
+            raise RuntimeError(f"{path} not built (reference source tree unavailable?)")
+        self.L = C.CDLL(str(path))
+        for n, (r, a) in self._sig.items():
+            f = getattr(self.L, n)
+            f.restype = r
+            f.argtypes = a
+        self.L.ref_setup(0)
+        self.dims = tuple(dims)
+        self.sizeh = self.L.ref_sizeh()
+
+    def phases(self, im_chem_pot=0.0):
+        ph = np.zeros((8, self.sizeh))
+        self.L.ref_calc_phases(_p(ph), im_chem_pot, 1.0)
+        return ph
+
+    def Deo(self, u, inp, ph):
+        out = np.zeros((3, self.sizeh), np.complex128)
+        self.L.ref_Deo(_p(u), _p(out), _p(inp), _p(ph))
+        return out
+
+    def Doe(self, u, inp, ph):
+        out = np.zeros((3, self.sizeh), np.complex128)
+        self.L.ref_Doe(_p(u), _p(out), _p(inp), _p(ph))
+        return out
+
+    def mdagm(self, u, inp, ph, mass, shift=0.0):
+        out = np.zeros((3, self.sizeh), np.complex128)
+        tmp = np.zeros_like(out)
+        self.L.ref_mdagm_shifted(_p(u), _p(out), _p(inp), _p(tmp), _p(ph), mass, shift)
+        return out
+
+    def cg(self, u, ph, mass, b, res, max_cg=10000, shift=0.0, restart=10000, x0=None):
+        x = np.zeros((3, self.sizeh), np.complex128) if x0 is None else x0.copy()
+        n = C.c_int(0)
+        self.L.ref_set_restart(restart)
+        st = self.L.ref_cg(_p(u), _p(ph), mass, _p(x), _p(b), res, max_cg, shift, C.byref(n))
+        return st, n.value, x
+
+    def cgm(self, u, ph, mass, a0, a, shifts, b, res, max_cg=10000):
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        shifts = np.ascontiguousarray(shifts, dtype=np.float64)
+        xs = np.zeros((len(shifts), 3, self.sizeh), np.complex128)
+        n = C.c_int(0)
+        st = self.L.ref_cgm(_p(u), _p(ph), mass, len(shifts), a0, _p(a), _p(shifts), _p(xs), _p(b), res, max_cg,
+                            C.byref(n))
+        return st, n.value, xs
+
+    def recombine(self, xs, b, a0, a):
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        out = np.zeros((3, self.sizeh), np.complex128)
+        self.L.ref_recombine(_p(xs), _p(b), _p(out), len(a), a0, _p(a))
+        return out

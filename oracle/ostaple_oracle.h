@@ -1,0 +1,43 @@
+/* ostaple_oracle.h -- CPU restatement of the reference's staggered-fermion
+ * hot path (GPU-LQCD/OpenStaPLE), used ONLY as the parity checker of the
+ * tests and as the CPU baseline of bench.py.  The product never links it.
+ *
+ * Parity pin: every function here is checked against the reference's own C
+ * sources compiled from source (oracle/Makefile.ref -> oracle/_ref) and
+ * against the golden vectors committed under tests/golden/, which were
+ * produced by that compiled reference.
+ *
+ * Layouts are the reference's SoA layouts with a run-time lattice:
+ *   vec3   : 3 x sizeh double complex
+ *   su3    : 9 x sizeh double complex (rows r0,r1,r2 of columns c0,c1,c2)
+ *   links  : 8 x su3, index 2*mu + parity
+ *   phases : 8 x sizeh double (angles)
+ *   tamat  : 3 x sizeh complex (c01,c02,c12) + 2 x sizeh double (ic00,ic11)
+ *   thmat  : 3 x sizeh complex (c01,c02,c12) + 2 x sizeh double (rc00,rc11)
+ */
+#ifndef OSTAPLE_ORACLE_H_
+#define OSTAPLE_ORACLE_H_
+
+#include <complex.h>
+
+typedef double complex ocplx;
+
+int orc_init(int n0, int n1, int n2, int n3);   /* returns sizeh */
+int orc_sizeh(void);
+void orc_set_threads(int n);
+
+void orc_calc_phases(double *phases, double im_chem_pot);
+void orc_Deo(const ocplx *u, ocplx *out, const ocplx *in, const double *ph);
+void orc_Doe(const ocplx *u, ocplx *out, const ocplx *in, const double *ph);
+void orc_mdagm(const ocplx *u, ocplx *out, const ocplx *in, ocplx *tmp, const double *ph, double m2);
+
+double orc_norm2(const ocplx *a);
+double orc_rdot(const ocplx *a, const ocplx *b);
+
+int orc_cg(const ocplx *u, const double *ph, double mass, ocplx *x, const ocplx *b, double res, int max_cg,
+           double shift, int restart_every, int *cg_out);
+int orc_cgm(const ocplx *u, const double *ph, double mass, int order, const double *ra_b, ocplx *xs,
+            const ocplx *b, double res, int max_cg, int *cg_out);
+void orc_recombine(const ocplx *xs, const ocplx *b, ocplx *out, int order, double a0, const double *a);
+
+#endif

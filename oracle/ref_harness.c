@@ -1,0 +1,248 @@
+/* ref_harness.c -- flat C entry points around the reference's OWN compiled
+ * double-precision hot-path sources, for use as a test oracle only.
+ *
+ * This file is linked with the UNMODIFIED reference sources (compiled from
+ * where they lie, see oracle/Makefile.ref) into oracle/_ref/libref_<dims>.so,
+ * one library per lattice size because the reference fixes the lattice at
+ * compile time (src/OpenAcc/geometry.h:28, src/Mpi/geometry_multidev.h:78-85).
+ * It supplies the globals the reference's host program would normally define
+ * and wraps the structured calls into pointer-only signatures that ctypes can
+ * drive from numpy buffers.  Nothing in the product links or loads this.
+ *
+ * Buffers follow the reference SoA layouts exactly:
+ *   vec3_soa  = 3 x sizeh complex double         (struct_c_def.h:16-20)
+ *   su3_soa   = 3 rows x vec3_soa                (struct_c_def.h:37-44)
+ *   links     = su3_soa[8], index 2*mu+parity    (geometry_multidev.h:284-296)
+ *   phases    = double_soa[8]                    (backfield.c:20-187)
+ *   tamat_soa = c01,c02,c12 complex + ic00,ic11  (struct_c_def.h:47-53)
+ *   thmat_soa = c01,c02,c12 complex + rc00,rc11  (struct_c_def.h:54-60)
+ */
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "../Include/common_defines.h"
+#include "../Mpi/multidev.h"
+#include "./action.h"
+#include "./geometry.h"
+#include "./struct_c_def.h"
+#include "./fermion_matrix.h"
+#include "./fermionic_utilities.h"
+#include "./inverter_full.h"
+#include "./inverter_multishift_full.h"
+#include "./inverter_package.h"
+#include "./stouting.h"
+#include "./fermion_force.h"
+#include "./fermion_force_utilities.h"
+#include "./backfield.h"
+#include "./backfield_parameters.h"
+#include "./su3_utilities.h"
+#include "./plaquettes.h"
+#include "./md_parameters.h"
+#include "../Include/debug.h"
+#include "../Include/inverter_tricks.h"
+#include "../Include/fermion_parameters.h"
+#include "../DbgTools/dbgtools.h"
+#include "./su3_measurements.h"
+#include "./sp_struct_c_def.h"
+#include "./sp_alloc_vars.h"
+
+/* ---- globals a reference host program defines (main.c / alloc_vars.c) ---- */
+int verbosity_lv = 0;
+action_param act_params;
+dev_info devinfo;
+int multishift_invert_iterations;
+su3_soa *auxbis_conf_acc, *glocal_staples;
+tamat_soa *gipdot, *aux_ta, *ipdot_f_old;
+thmat_soa *aux_th;
+su3_soa_f *conf_acc_f;
+vec3_soa_f *ferm_shiftmulti_acc_f, *aux1_f;
+debug_settings_t debug_settings;
+md_param md_parameters;
+int md_dbg_print_count, md_diag_count_fermion, ipdot_f_reset, nMdInversionPerformed;
+
+/* stubs for diagnostics that the wrapped paths never reach at verbosity 0 */
+void check_unitarity_device(const su3_soa *u, double *mx, double *avg) { *mx = 0; *avg = 0; }
+double calc_force_norm(const tamat_soa *t) { return 0.0; }
+double calc_diff_force_norm(const tamat_soa *a, const tamat_soa *b) { return 0.0; }
+void copy_ipdot_into_old(const tamat_soa *a, tamat_soa *b) {}
+void dbg_print_su3_soa(su3_soa *const conf, const char *n, int i) {}
+void convert_double_to_float_su3_soa(const su3_soa *d, su3_soa_f *f) {}
+int inverter_multishift_wrapper(inverter_package ip, ferm_param *pars, RationalApprox *approx,
+                                vec3_soa *out, const vec3_soa *in, double res, int max_cg, int ci)
+{ return 0; }
+
+static void *xalloc(size_t n)
+{
+  void *p = NULL;
+  if (posix_memalign(&p, 128, n)) { fprintf(stderr, "ref_harness: OOM\n"); exit(2); }
+  memset(p, 0, n);
+  return p;
+}
+
+/* ---- geometry ---- */
+int ref_sizeh(void) { return sizeh; }
+void ref_dims(int *d) { d[0] = nd0; d[1] = nd1; d[2] = nd2; d[3] = nd3; }
+
+void ref_setup(int verbosity)
+{
+  verbosity_lv = verbosity;
+  devinfo.myrank = 0; devinfo.nranks = 1;
+  geom_par.gnx = nd0; geom_par.gny = nd1; geom_par.gnz = nd2; geom_par.gnt = nd3;
+  geom_par.xmap = 0; geom_par.ymap = 1; geom_par.zmap = 2; geom_par.tmap = 3;
+  set_geom_glv(&geom_par);
+  compute_nnp_and_nnm_openacc();
+  inverter_tricks.restartingEvery = 10000;
+  inverter_tricks.useMixedPrecision = 0;
+  inverter_tricks.mixedPrecisionDelta = 0.1;
+  inverter_tricks.singlePInvAccelMultiInv = 0;
+  act_params.stout_steps = 2;
+  act_params.stout_rho = 0.15;
+  gl_stout_rho = 0.15;
+}
+
+void ref_set_restart(int every) { inverter_tricks.restartingEvery = every; }
+
+/* staggered phases + APBC (+ optional imaginary chemical potential), no B/E. */
+void ref_calc_phases(double *phases, double im_chem_pot, double charge)
+{
+  bf_param bf;
+  memset(&bf, 0, sizeof(bf));
+  calc_u1_phases((double_soa *)phases, bf, im_chem_pot, charge);
+}
+
+/* ---- Dirac operator ---- */
+void ref_Deo(const double *u, double *out, const double *in, const double *ph)
+{ acc_Deo((const su3_soa *)u, (vec3_soa *)out, (const vec3_soa *)in, (const double_soa *)ph); }
+
+void ref_Doe(const double *u, double *out, const double *in, const double *ph)
+{ acc_Doe((const su3_soa *)u, (vec3_soa *)out, (const vec3_soa *)in, (const double_soa *)ph); }
+
+static void make_fp(ferm_param *fp, double *ph, double mass)
+{
+  memset(fp, 0, sizeof(*fp));
+  fp->ferm_mass = mass;
+  fp->phases = (double_soa *)ph;
+}
+
+void ref_mdagm_shifted(const double *u, double *out, const double *in, double *temp,
+                       double *ph, double mass, double shift)
+{
+  ferm_param fp; make_fp(&fp, ph, mass);
+  fermion_matrix_multiplication_shifted((const su3_soa *)u, (vec3_soa *)out, (const vec3_soa *)in,
+                                        (vec3_soa *)temp, &fp, shift);
+}
+
+/* ---- BLAS / reductions ---- */
+double ref_l2norm2(const double *v) { return l2norm2_global((const vec3_soa *)v); }
+double ref_real_scal_prod(const double *a, const double *b)
+{ return real_scal_prod_global((const vec3_soa *)a, (const vec3_soa *)b); }
+void ref_scal_prod(const double *a, const double *b, double *re_im)
+{
+  d_complex z = scal_prod_global((const vec3_soa *)a, (const vec3_soa *)b);
+  re_im[0] = creal(z); re_im[1] = cimag(z);
+}
+
+/* ---- single-shift CG (inverter_full.c:19-132) ---- */
+int ref_cg(const double *u, double *ph, double mass, double *solution, const double *in,
+           double res, int max_cg, double shift, int *cg_out)
+{
+  size_t vb = sizeof(vec3_soa);
+  vec3_soa *r = xalloc(vb), *h = xalloc(vb), *s = xalloc(vb), *p = xalloc(vb);
+  ferm_param fp; make_fp(&fp, ph, mass);
+  int st = ker_invert_openacc((const su3_soa *)u, &fp, (vec3_soa *)solution, (const vec3_soa *)in,
+                              res, r, h, s, p, max_cg, shift, cg_out);
+  free(r); free(h); free(s); free(p);
+  return st;
+}
+
+/* ---- multi-shift CG (inverter_multishift_full.c:23-252) ---- */
+int ref_cgm(const double *u, double *ph, double mass, int order, double a0, const double *a,
+            const double *b, double *out, const double *in, double res, int max_cg, int *cg_out)
+{
+  size_t vb = sizeof(vec3_soa);
+  vec3_soa *r = xalloc(vb), *h = xalloc(vb), *s = xalloc(vb), *p = xalloc(vb);
+  vec3_soa *sf = xalloc(vb * (size_t)order);
+  ferm_param fp; make_fp(&fp, ph, mass);
+  RationalApprox ra; memset(&ra, 0, sizeof(ra));
+  ra.approx_order = order; ra.RA_a0 = a0;
+  for (int i = 0; i < order; i++) { ra.RA_a[i] = a[i]; ra.RA_b[i] = b[i]; }
+  int st = multishift_invert((const su3_soa *)u, &fp, &ra, (vec3_soa *)out, (const vec3_soa *)in,
+                             res, r, h, s, p, sf, max_cg, cg_out);
+  free(r); free(h); free(s); free(p); free(sf);
+  return st;
+}
+
+void ref_recombine(const double *xs, const double *in, double *out, int order, double a0,
+                   const double *a)
+{
+  RationalApprox ra; memset(&ra, 0, sizeof(ra));
+  ra.approx_order = order; ra.RA_a0 = a0;
+  for (int i = 0; i < order; i++) ra.RA_a[i] = a[i];
+  recombine_shifted_vec3_to_vec3((const vec3_soa *)xs, (const vec3_soa *)in, (vec3_soa *)out, &ra);
+}
+
+/* ---- stout smearing (stouting.c:36-165) ---- */
+void ref_stout_isotropic(const double *u, double *uprime, double rho)
+{
+  gl_stout_rho = rho;
+  su3_soa *stap = xalloc(8 * sizeof(su3_soa));
+  su3_soa *aux = xalloc(8 * sizeof(su3_soa));
+  tamat_soa *ta = xalloc(8 * sizeof(tamat_soa));
+  stout_isotropic((const su3_soa *)u, (su3_soa *)uprime, stap, aux, ta, 0);
+  free(stap); free(aux); free(ta);
+}
+
+/* the staples times C_ZERO that stout uses (plaquettes.c:196-259) */
+void ref_staples(const double *u, double *stap)
+{
+  set_su3_soa_to_zero((su3_soa *)stap);
+  calc_loc_staples_nnptrick_all_onlyferms((const su3_soa *)u, (su3_soa *)stap);
+}
+
+/* Q_A = rho/C_ZERO * TA(U*C) (su3_utilities.c:210-239) */
+void ref_rho_ta(const double *u, const double *stap, double *qa, double rho)
+{
+  gl_stout_rho = rho;
+  RHO_times_conf_times_staples_ta_part((const su3_soa *)u, (const su3_soa *)stap, (tamat_soa *)qa, 0);
+}
+
+/* ---- fermion force pieces (fermion_force_utilities.c:30-201) ---- */
+void ref_force_outer_products(const double *u, double *aux_u, const double *xs, double *ph,
+                              double mass, int order, const double *a)
+{
+  size_t vb = sizeof(vec3_soa);
+  vec3_soa *s = xalloc(vb), *h = xalloc(vb);
+  ferm_param fp; make_fp(&fp, ph, mass);
+  fp.approx_md.approx_order = order;
+  for (int i = 0; i < order; i++) fp.approx_md.RA_a[i] = a[i];
+  ker_openacc_compute_fermion_force((const su3_soa *)u, (su3_soa *)aux_u, (const vec3_soa *)xs,
+                                    s, h, &fp);
+  free(s); free(h);
+}
+
+void ref_backfield_times_force(double *ph, const double *auxmat, double *pseudo_ipdot)
+{
+  ferm_param fp; make_fp(&fp, ph, 0.0);
+  multiply_backfield_times_force(&fp, (const su3_soa *)auxmat, (su3_soa *)pseudo_ipdot);
+}
+
+/* Sigma' -> Sigma through one stout level (fermion_force.c:52-162) */
+void ref_sigma_prime_to_sigma(double *sigma, const double *u, double rho)
+{
+  gl_stout_rho = rho;
+  thmat_soa *lam = xalloc(8 * sizeof(thmat_soa));
+  tamat_soa *qa = xalloc(8 * sizeof(tamat_soa));
+  su3_soa *tmp = xalloc(8 * sizeof(su3_soa));
+  compute_sigma_from_sigma_prime_backinto_sigma_prime((su3_soa *)sigma, lam, qa, (const su3_soa *)u,
+                                                      tmp, 0);
+  free(lam); free(qa); free(tmp);
+}
+
+void ref_conf_times_force_ta(const double *u, const double *auxmat, double *ipdot)
+{
+  multiply_conf_times_force_and_take_ta_nophase((const su3_soa *)u, (const su3_soa *)auxmat,
+                                                (tamat_soa *)ipdot);
+}
+
+void ref_set_tamat_zero(double *t) { set_tamat_soa_to_zero((tamat_soa *)t); }
