@@ -1,0 +1,342 @@
+#!/usr/bin/env python3
+"""Benchmark of the staggered M^+M solve on one GB300.
+
+Workload: solve (M^+M) x = b with M^+M = m^2 - D_eo D_oe on a 32^4 lattice,
+m = 0.01, to an FP64 true residual sqrt(|b - M^+M x|^2/|b|^2) <= 1e-10 -- the
+configuration the headline metric is quoted on.  Links are seeded
+U = exp(i*0.3*H) (H Gaussian traceless Hermitian per link), staggered phases
+with antiperiodic time boundary, a Gaussian source on the even sites.
+
+A step is one complete solve.  `value` is solves per second over all GPUs
+(independent replicas, one per rank, weak scaling), timed with CUDA events on
+the solver's stream with all inputs resident in HBM; `e2e` is the same solve
+through the reference-facing C entry points with pinned host buffers, the
+host->device copies of links, phases, source and guess and the device->host
+copy of the solution inside the timed region.  The plain FP64 CG
+(ker_invert_openacc) is timed beside it.
+
+--impl reference times the reference's CPU implementation of the same solve
+(its FP64 CG, restated as the oracle port and run with all host threads) on
+rank 0.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+PEAKS_FILE = ROOT / "MEASURED_PEAKS.json"
+PROFILE_TRAFFIC = ROOT / "profiles" / "traffic.json"
+FALLBACK_HBM = 6800.0
+
+# algorithmic bytes per output site of one hop application
+BYTES_F32_SIGN = 8 * 12 * 4 + 8 * 1 + 3 * 8 + 3 * 8      # links(2 rows) + sign bytes + in + out = 440
+BYTES_F64_ANGLE = 8 * 12 * 8 + 8 * 8 + 3 * 16 + 3 * 16   # links(2 rows) + angles + in + out = 928
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--dims", default="32,32,32,32")
+    ap.add_argument("--mass", type=float, default=0.01)
+    ap.add_argument("--eps", type=float, default=0.3)
+    ap.add_argument("--res", type=float, default=1e-10)
+    ap.add_argument("--seed", type=int, default=2024)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--skip-fp64", action="store_true", help="skip the plain FP64 CG arm (profiling runs)")
+    return ap.parse_args()
+
+
+def peaks():
+    if PEAKS_FILE.exists():
+        d = json.loads(PEAKS_FILE.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return FALLBACK_HBM, "fallback"
+
+
+class ClockSampler:
+    """Samples nvidia-smi SM clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for s in self.samples:
+            for k, n in enumerate(names):
+                if len(s) > 5 + k and s[5 + k].lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.samples)}
+
+
+def make_inputs(dims, seed, eps):
+    from openstaple_gb300 import fields as F
+    u = F.random_su3_links(dims, seed, eps=eps)
+    ph = F.staggered_phases(dims)
+    b = F.gaussian_vec3(dims, seed + 1)
+    return u, ph, b
+
+
+def cpu_cg_rate(dims, u, ph, b, mass, res, fp64_iters, budget_s=20.0):
+    """Times the oracle port of the reference's FP64 CG (all host threads) on a
+    bounded number of iterations and extrapolates to the full solve with the
+    iteration count of the identical FP64 algorithm."""
+    from oracle import Oracle
+    threads = os.cpu_count() or 1
+    o = Oracle(dims, threads=threads)
+    t0 = time.perf_counter()
+    o.cg(u, ph, mass, b, res, max_cg=2, restart=2)
+    per_iter = (time.perf_counter() - t0) / 2.0
+    n = int(max(3, min(fp64_iters, budget_s / max(per_iter, 1e-6))))
+    t0 = time.perf_counter()
+    o.cg(u, ph, mass, b, res, max_cg=n, restart=n)
+    per_iter = (time.perf_counter() - t0) / n
+    solve_s = per_iter * fp64_iters
+    return dict(value=1.0 / solve_s, unit="solves/s", cores=threads, kind="port",
+                sample=f"{n} FP64 CG iterations of the oracle port on {'x'.join(map(str, dims))} "
+                       f"({per_iter * 1e3:.1f} ms/iteration) x {fp64_iters} iterations per solve")
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    dims = tuple(int(x) for x in args.dims.split(","))
+    from oracle import Oracle
+    threads = os.cpu_count() or 1
+    u, ph, b = make_inputs(dims, args.seed, args.eps)
+    o = Oracle(dims, threads=threads)
+    times, iters = [], None
+    for k in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        st, n, x = o.cg(u, ph, args.mass, b, args.res)
+        dt = time.perf_counter() - t0
+        iters = n
+        if k >= args.warmup:
+            times.append(dt)
+        if k == 0 and dt * (args.warmup + args.steps) > 300:
+            # bounded samples: keep the run within minutes
+            args.steps, args.warmup = 1, 0
+            times = [dt]
+            break
+    ms = 1e3 * float(np.mean(times))
+    val = 1e3 / ms
+    line = {"impl": "reference", "metric": "MdagM solves/s to FP64 true residual 1e-10", "value": val,
+            "unit": "solves/s", "n_gpus": args.gpus, "steps": len(times), "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"MdagM CG solve {'x'.join(map(str, dims))} m={args.mass} res={args.res}",
+                       "solver": "FP64 CG (inverter_full.c:19-132), oracle port, all host threads",
+                       "cg_iterations": iters},
+            "cpu_baseline": {"value": val, "unit": "solves/s", "cores": threads, "kind": "port",
+                             "sample": f"{len(times)} full FP64 CG solves"},
+            "e2e": {"value": val, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import ctypes as C
+    import torch
+    import torch.distributed as dist
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl")
+    from openstaple_gb300 import api
+    from openstaple_gb300.native import lib
+    L = lib()
+    dims = tuple(int(x) for x in args.dims.split(","))
+    u, ph, b = make_inputs(dims, args.seed + 17 * rank, args.eps)
+    lat = api.Lattice(dims)
+    stream = torch.cuda.Stream()
+    L.ostaple_set_stream(C.c_void_p(stream.cuda_stream))
+    x = lat.vec3()
+    for a in (u, ph, b, x):
+        lat.present(a)
+    zero = np.zeros_like(x)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # plain FP64 CG (the reference algorithm on the GPU), timed once after a warm-up
+    work = [lat.vec3() for _ in range(4)]
+    for a in work:
+        lat.present(a, copy=False)
+    fp = api.make_ferm_param(args.mass, ph)
+    fp64 = {"ms": float("nan"), "iters": 0, "status": -1}
+    for k in range(0 if args.skip_fp64 else 2):
+        L.set_vec3_soa_to_zero(x.ctypes.data)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        st, n = api.ker_invert_openacc(u, fp, x, b, args.res, *work, 100000, 0.0)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        fp64 = dict(ms=e0.elapsed_time(e1), iters=n, status=st)
+    for a in work:
+        lat.release(a)
+
+    def solve():
+        L.set_vec3_soa_to_zero(x.ctypes.data)
+        return api.invert_mixed(u, ph, args.mass, 0.0, x, b, args.res, 100000, 0)
+
+    for _ in range(args.warmup):
+        info = solve()
+    barrier()
+    launches0 = L.ostaple_kernel_launches()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        barrier()
+        e0.record(stream)
+        infos = [solve() for _ in range(args.steps)]
+        e1.record(stream)
+        barrier()
+    launches = L.ostaple_kernel_launches() - launches0
+    ms = e0.elapsed_time(e1) / args.steps
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * 1e3 / ms
+    ok = all(i["status"] == 1 and i["true_res"] <= args.res for i in infos)
+
+    # roofline of the dominant kernel (the FP32 hop of the mixed solver), timed alone
+    hbm, peak_kind = peaks()
+    kms = C.c_double(0)
+    L.ostaple_time_kernel(1, u.ctypes.data, ph.ctypes.data, 50, C.byref(kms))
+    achieved = BYTES_F32_SIGN * lat.sizeh / (kms.value * 1e-3) / 1e9
+    traffic = None
+    if PROFILE_TRAFFIC.exists():
+        tr = json.loads(PROFILE_TRAFFIC.read_text())
+        key = f"dslash_f32_doe_{'x'.join(map(str, dims))}"
+        if key in tr:
+            traffic = tr[key]["bytes_per_launch"]
+    k64 = C.c_double(0)
+    L.ostaple_time_kernel(0, u.ctypes.data, ph.ctypes.data, 10, C.byref(k64))
+    fp64_peak = C.c_double(0)
+    L.ostaple_probe_fma_tflops(1, C.byref(fp64_peak))
+    dslash64_flops = 2 * (8 * 60 + 6) * lat.sizeh  # executed FP64 FMAs (x2) per application
+
+    # end to end through the C entry points with pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        for a in (u, ph, b, x):
+            L.ostaple_pin_host(a.ctypes.data, a.nbytes)
+        h2d = u.nbytes + ph.nbytes + b.nbytes + x.nbytes
+        d2h = x.nbytes
+        times = []
+        for k in range(args.warmup + args.steps):
+            x[...] = zero
+            barrier()
+            t0 = time.perf_counter()
+            for a in (u, ph, b, x):
+                lat.update_device(a)
+            api.invert_mixed(u, ph, args.mass, 0.0, x, b, args.res, 100000, 0)
+            lat.update_host(x)
+            dt = time.perf_counter() - t0
+            if k >= args.warmup:
+                times.append(dt)
+        e2e_ms = 1e3 * float(np.mean(times))
+        if world > 1:
+            t = torch.tensor([e2e_ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e2e_ms = float(t.item())
+        e2e = {"value": world * 1e3 / e2e_ms, "unit": "solves/s", "ms_per_step": e2e_ms,
+               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline and fp64["iters"] > 0:
+        cpu = cpu_cg_rate(dims, u, ph, b, args.mass, args.res, fp64["iters"])
+
+    if rank == 0:
+        line = {
+            "metric": "MdagM solves/s to FP64 true residual 1e-10", "value": value, "unit": "solves/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+            "data": "synthetic (seeded exp(i*0.3*H) links, Gaussian source)",
+            "config": {"workload": f"MdagM solve {'x'.join(map(str, dims))} m={args.mass} to FP64 true residual "
+                                   f"{args.res}",
+                       "solver": "mixed-precision CG (FP32 iteration, FP64 reliable updates, CUDA-graph chunks)",
+                       "iterations": infos[-1]["iters"], "reliable_updates": infos[-1]["n_reliable"],
+                       "true_residual": infos[-1]["true_res"], "all_converged": ok,
+                       "plain_fp64_cg": {"ms": fp64["ms"], "iterations": fp64["iters"], "status": fp64["status"]},
+                       "speedup_vs_plain_fp64_cg": fp64["ms"] / ms,
+                       "l2": "inputs larger than L2 (FP32 links 201 MB, FP64 links 604 MB > 129 MB)",
+                       "parallelism": f"replicas x{world}"},
+            "roofline": {"kernel": "k_mx_doe (FP32 D_oe, compact links + sign bytes)", "bound": "hbm",
+                         "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                         "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+                         "traffic": traffic, "bytes_per_site": BYTES_F32_SIGN, "ms_per_launch": kms.value},
+            "fp64_dslash": {"ms_per_launch": k64.value,
+                            "hbm_gbs": BYTES_F64_ANGLE * lat.sizeh / (k64.value * 1e-3) / 1e9,
+                            "fp64_tflops_executed": dslash64_flops / (k64.value * 1e-3) / 1e12,
+                            "fp64_fma_peak_tflops_measured": fp64_peak.value},
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "gpu_launches": int(launches),
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(line))
+    lat.close()
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -141,6 +141,19 @@ int ostaple_update_host(void *host, size_t bytes);
 /* acc_deviceptr(): device mirror of a registered host address, or NULL */
 void *ostaple_deviceptr(const void *host);
 
+/* Number of kernels the library has launched (graph replays count the
+ * kernels they contain).  No reference counterpart. */
+unsigned long long ostaple_kernel_launches(void);
+/* Page-locks a host range so that update_device/update_host copies run at
+ * full host-link bandwidth (cudaHostRegister).  No reference counterpart. */
+int ostaple_pin_host(void *host, size_t bytes);
+int ostaple_unpin_host(void *host);
+/* Mean milliseconds of one launch of a hot kernel, timed with CUDA events on
+ * its own stream: which = 0 FP64 D_eo (as acc_Deo), 1 FP32 D_oe of the mixed
+ * solver, 2 FP32 fused D_eo + M^+M epilogue + <p,Ap>.  No reference
+ * counterpart (measurement hook). */
+int ostaple_time_kernel(int which, const su3_soa *u, const double_soa *phases, int reps, double *ms);
+
 /* Measured FMA throughput of this device in TFLOP/s (fp64 != 0: FP64, else
  * FP32); the ceiling of the compute-bound FP64 kernels.  No reference
  * counterpart. */
@@ -214,6 +227,32 @@ int multishift_invert(const su3_soa *u, ferm_param *pars, RationalApprox *approx
 /* out = a0 in + sum_i a_i in_shifted[i] (inverter_multishift_full.h:30-33) */
 void recombine_shifted_vec3_to_vec3(const vec3_soa *in_shifted, const vec3_soa *in, vec3_soa *out,
                                     const RationalApprox *approx);
+
+/* Mixed-precision CG: FP32 iteration, FP64 solution and reliable updates of
+ * the residual when |r|^2 < inverter_tricks.mixedPrecisionDelta * max|r|^2
+ * (inverter_mixedp.c:41-48).  FP32 links come from ip.u_f when set (the
+ * reference's converted su3_soa_f), else from ip.u; ip's FP32/FP64 parking
+ * vectors are used when set. */
+int inverter_mixed_precision(inverter_package ip, ferm_param *pars, vec3_soa *solution, const vec3_soa *in,
+                             double res, const int max_cg, double shift, int *cg_return);
+/* Exits the process on a failure marked CONVERGENCE_CRITICAL
+ * (inverter_wrappers.c:24-39). */
+void convergence_messages(int conv_importance, int inverter_status);
+/* Dispatches to inverter_mixed_precision or ker_invert_openacc by
+ * inverter_tricks.useMixedPrecision; returns the iteration count
+ * (inverter_wrappers.c:117-160). */
+int inverter_wrapper(inverter_package ip, ferm_param *pars, vec3_soa *out, const vec3_soa *in, double res,
+                     int max_cg, double shift, int convergence_importance);
+
+/* Mixed-precision CG that iterates until the FP64 true residual
+ * sqrt(|b - (M^+M + shift) x|^2 / |b|^2) is <= res (or max_iter), with a
+ * reliable update every `reliable_every` iterations (0: the reference's
+ * delta criterion).  Reports iterations, the final FP64 true residual and
+ * the number of reliable updates.  Extends inverter_mixed_precision; no
+ * reference counterpart. */
+int ostaple_invert_mixed(const su3_soa *u, const double_soa *phases, double mass, double shift,
+                         vec3_soa *solution, const vec3_soa *in, double res, int max_iter, int reliable_every,
+                         int *iters, double *true_res, int *n_reliable);
 
 #ifdef __cplusplus
 }

@@ -15,7 +15,7 @@ from typing import Sequence
 
 import numpy as np
 
-from .native import FermParam, RationalApprox, check, inverter_tricks, lib
+from .native import FermParam, InverterPackage, RationalApprox, check, inverter_tricks, lib
 
 
 def ptr(a) -> int:
@@ -166,3 +166,37 @@ def recombine_shifted_vec3_to_vec3(in_shifted, inp, out, approx: RationalApprox)
 
 def set_restarting_every(n: int) -> None:
     inverter_tricks().restartingEvery = int(n)
+
+
+def make_inverter_package(u, loc_r=None, loc_h=None, loc_s=None, loc_p=None, u_f=None, loc_r_f=None, loc_h_f=None,
+                          loc_s_f=None, loc_p_f=None, out_f=None, ferm_shift_temp=None, nshifts=0) -> InverterPackage:
+    """setup_inverter_package_dp/_sp (inverter_package.c:17-77) in one call;
+    unset parking vectors make the library use its own workspace."""
+    ip = InverterPackage()
+    ip.u = ptr(u)
+    opt = lambda a: None if a is None else ptr(a)  # noqa: E731
+    ip.u_f = opt(u_f)
+    ip.loc_r, ip.loc_h, ip.loc_s, ip.loc_p = opt(loc_r), opt(loc_h), opt(loc_s), opt(loc_p)
+    ip.loc_r_f, ip.loc_h_f, ip.loc_s_f, ip.loc_p_f = opt(loc_r_f), opt(loc_h_f), opt(loc_s_f), opt(loc_p_f)
+    ip.out_f = opt(out_f)
+    ip.ferm_shift_temp = opt(ferm_shift_temp)
+    ip.nshifts = nshifts
+    return ip
+
+
+def inverter_mixed_precision(ip: InverterPackage, pars: FermParam, solution, inp, res: float, max_cg: int,
+                             shift: float) -> tuple[int, int]:
+    cg = C.c_int(0)
+    st = lib().inverter_mixed_precision(ip, C.byref(pars), ptr(solution), ptr(inp), res, max_cg, shift, C.byref(cg))
+    check(0, "inverter_mixed_precision")
+    return st, cg.value
+
+
+def invert_mixed(u, phases, mass: float, shift: float, solution, inp, res: float = 1e-10, max_iter: int = 100000,
+                 reliable_every: int = 0) -> dict:
+    """Mixed-precision solve to an FP64 true residual <= res."""
+    it, nrel, tr = C.c_int(0), C.c_int(0), C.c_double(0)
+    st = lib().ostaple_invert_mixed(ptr(u), ptr(phases), mass, shift, ptr(solution), ptr(inp), res, max_iter,
+                                    reliable_every, C.byref(it), C.byref(tr), C.byref(nrel))
+    check(0, "ostaple_invert_mixed")
+    return dict(status=st, iters=it.value, true_res=tr.value, n_reliable=nrel.value)

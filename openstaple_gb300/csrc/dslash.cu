@@ -43,7 +43,7 @@ dslash_kernel(Geom g, LinkView<typename cplx_t<T>::type> u, typename cplx_t<T>::
 template <typename T, int P, int PH, int EPI>
 static void launch_one(const DslashArgs<T>& a) {
   const Geom& g = rt().g;
-  LinkView<typename cplx_t<T>::type> u{a.u, g.sizeh};
+  LinkView<typename cplx_t<T>::type> u{a.u, g.sizeh, a.compact_links ? 6 : 9};
   dslash_kernel<T, P, PH, EPI><<<blocks_for(g.sizeh, DSLASH_THREADS), DSLASH_THREADS, 0, a.stream>>>(
       g, u, a.out, a.in, a.phases, a.in0, a.mass2);
   OST_LAUNCH_CHECK();

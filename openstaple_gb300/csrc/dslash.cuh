@@ -69,13 +69,18 @@ OST_D void apply_angle_phase(typename cplx_t<T>::type v[3], T arg,
   }
 }
 
-// Link field access: 8 su3_soa blocks, each 9*sizeh complex (row-major rows
-// r0,r1,r2 of vec3_soa columns c0,c1,c2).
+// Link field access: 8 blocks, one per (mu, parity).  The reference layout
+// (su3_soa) holds 9 complex arrays per block (rows r0,r1,r2 of columns
+// c0,c1,c2; rows_per_dir = 9); the library's internal single-precision copy
+// keeps only the two rows the kernels read (rows_per_dir = 6).
 template <typename C>
 struct LinkView {
   const C* base;
   long sizeh;
-  OST_D const C* at(int dir, int row, int col) const { return base + (long(dir) * 9 + row * 3 + col) * sizeh; }
+  int rows_per_dir;
+  OST_D const C* at(int dir, int row, int col) const {
+    return base + (long(dir) * rows_per_dir + row * 3 + col) * sizeh;
+  }
 };
 
 template <typename C>

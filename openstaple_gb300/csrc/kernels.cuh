@@ -21,6 +21,7 @@ struct DslashArgs {
   const C* in0;               // EPI_MDAGM: the vector multiplied by mass2
   T mass2;
   cudaStream_t stream;
+  int compact_links = 0;      // 1: 6 complex arrays per direction (two rows only)
 };
 
 template <typename T> void launch_dslash(const DslashArgs<T>& a);

@@ -1,0 +1,418 @@
+// mixed.cu -- mixed-precision CG on (M^+M + shift): the iteration runs in
+// FP32 (links, vectors, Dslash; reductions accumulate in FP64), the solution
+// accumulates in FP64, and the residual is periodically recomputed in FP64
+// ("reliable updates", the reference's "magic touch", inverter_mixedp.c:41-181,
+// after arXiv:0911.3191).
+//
+// Per iteration four kernels run, all reading their scalars from device
+// memory (MixScal), so a chunk of iterations is captured once as a CUDA graph
+// and replayed; the host polls the flags once per chunk.  Each kernel returns
+// immediately when the recursion has converged (done) or asks for a reliable
+// update (need_rel), so replaying a chunk past either point does no work.
+#include <cmath>
+#include <cstring>
+#include "dslash.cuh"
+#include "kernels.cuh"
+#include "mixed.cuh"
+#include "reduce.cuh"
+#include "runtime.cuh"
+
+namespace ost {
+
+static constexpr int MX_THREADS = 128;
+
+OST_D bool halted(const MixScal* s) { return (*(volatile const int*)&s->done) | (*(volatile const int*)&s->need_rel); }
+
+// ---- preparation kernels ----
+__global__ void k_links_f32(const double2* __restrict__ u64, float2* __restrict__ u32, long sh) {
+  const long n = 8L * 6 * sh;
+  for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n; i += long(gridDim.x) * blockDim.x) {
+    long dir = i / (6 * sh), rem = i - dir * 6 * sh;   // rem indexes rows 0..1 (6 arrays)
+    double2 v = __ldcs(u64 + dir * 9 * sh + rem);
+    u32[i] = make_float2(float(v.x), float(v.y));
+  }
+}
+
+void links_to_f32_compact(const double2* u64, float2* u32, long sh, cudaStream_t st) {
+  k_links_f32<<<8 * rt().num_sms, 256, 0, st>>>(u64, u32, sh);
+  OST_LAUNCH_CHECK();
+}
+
+__global__ void k_signs(const double* __restrict__ ph, unsigned char* sg, int* all_exact, long n) {
+  const unsigned long long PI = 0x400921FB54442D18ull;
+  bool ok = true;
+  for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n; i += long(gridDim.x) * blockDim.x) {
+    unsigned long long b = (unsigned long long)__double_as_longlong(ph[i]);
+    sg[i] = (b == PI) ? 1 : 0;
+    ok = ok && (b == 0 || b == PI);
+  }
+  if (!__all_sync(0xffffffffu, ok) && (threadIdx.x & 31) == 0) atomicAnd(all_exact, 0);
+}
+
+void phases_to_signs(const double* ph64, unsigned char* sg, int* all_exact, long sh, cudaStream_t st) {
+  k_signs<<<4 * rt().num_sms, 256, 0, st>>>(ph64, sg, all_exact, 8 * sh);
+  OST_LAUNCH_CHECK();
+}
+
+__global__ void k_ph32(const double* __restrict__ ph, float* out, long n) {
+  for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n; i += long(gridDim.x) * blockDim.x)
+    out[i] = float(ph[i]);
+}
+
+void phases_to_f32(const double* ph64, float* ph32, long sh, cudaStream_t st) {
+  k_ph32<<<4 * rt().num_sms, 256, 0, st>>>(ph64, ph32, 8 * sh);
+  OST_LAUNCH_CHECK();
+}
+
+// ---- FP32 iteration kernels ----
+// t = D_oe p
+template <int PH>
+__global__ void __launch_bounds__(MX_THREADS)
+k_mx_doe(Geom g, LinkView<float2> u, const void* __restrict__ ph, const float2* __restrict__ p,
+         float2* __restrict__ t, const MixScal* sc) {
+  if (halted(sc)) return;
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= g.sizeh) return;
+  float2 aux[3];
+  hop<float, 1, PH>(g, u, p, ph, idx, aux);
+#pragma unroll
+  for (int c = 0; c < 3; ++c) t[c * long(g.sizeh) + idx] = make_float2(0.5f * aux[c].x, 0.5f * aux[c].y);
+}
+
+// s = m2 p - D_eo t ; pAp = Re<p, s> ; alpha = delta / pAp
+template <int PH>
+__global__ void __launch_bounds__(MX_THREADS)
+k_mx_deo_dot(Geom g, LinkView<float2> u, const void* __restrict__ ph, const float2* __restrict__ t,
+             const float2* __restrict__ p, float2* __restrict__ s, MixScal* sc, ReduceWs ws) {
+  if (halted(sc)) return;
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  double v[1] = {0.0};
+  if (idx < g.sizeh) {
+    const float m2 = float(sc->m2);
+    float2 aux[3];
+    hop<float, 0, PH>(g, u, t, ph, idx, aux);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const long k = c * long(g.sizeh) + idx;
+      float2 pv = p[k];
+      float2 r = make_float2(fmaf(pv.x, m2, -0.5f * aux[c].x), fmaf(pv.y, m2, -0.5f * aux[c].y));
+      s[k] = r;
+      v[0] += double(pv.x) * double(r.x) + double(pv.y) * double(r.y);
+    }
+  }
+  double tot[1];
+  if (grid_reduce<1>(v, ws, tot)) {
+    sc->pAp = tot[0];
+    sc->alpha = sc->delta / tot[0];
+  }
+}
+
+// x_f += alpha p ; unless a reliable update is due: r -= alpha s, lambda = |r|^2,
+// beta = lambda / delta, delta = lambda.
+__global__ void k_mx_update(float4* __restrict__ xf, float4* __restrict__ r, const float4* __restrict__ p,
+                            const float4* __restrict__ s, long n4, MixScal* sc, ReduceWs ws) {
+  if (halted(sc)) return;
+  const double delta = sc->delta;
+  const double lm = sc->last_max > delta ? sc->last_max : delta;
+  const bool rel = sc->every > 0 ? ((sc->iter + 1) % sc->every == 0) : (delta < sc->frac * lm);
+  const float a = float(sc->alpha);
+  double v[1] = {0.0};
+  for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n4; i += long(gridDim.x) * blockDim.x) {
+    float4 pv = p[i], xv = xf[i];
+    xv.x = fmaf(a, pv.x, xv.x); xv.y = fmaf(a, pv.y, xv.y); xv.z = fmaf(a, pv.z, xv.z); xv.w = fmaf(a, pv.w, xv.w);
+    xf[i] = xv;
+    if (!rel) {
+      float4 sv = s[i], rv = r[i];
+      rv.x = fmaf(-a, sv.x, rv.x); rv.y = fmaf(-a, sv.y, rv.y); rv.z = fmaf(-a, sv.z, rv.z); rv.w = fmaf(-a, sv.w, rv.w);
+      r[i] = rv;
+      v[0] += double(rv.x) * rv.x + double(rv.y) * rv.y + double(rv.z) * rv.z + double(rv.w) * rv.w;
+    }
+  }
+  double tot[1];
+  if (grid_reduce<1>(v, ws, tot)) {
+    sc->iter += 1;
+    sc->last_max = lm;
+    if (rel) {
+      sc->need_rel = 1;
+    } else {
+      sc->lambda = tot[0];
+      sc->beta = tot[0] / delta;
+      sc->delta = tot[0];
+      if (tot[0] <= sc->target2 || sc->iter >= sc->max_iter) sc->done = 1;
+    }
+  }
+}
+
+// p = r + beta p
+__global__ void k_mx_pupdate(float4* __restrict__ p, const float4* __restrict__ r, long n4, const MixScal* sc,
+                             int guarded) {
+  if (guarded && halted(sc)) return;
+  const float b = float(sc->beta);
+  for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n4; i += long(gridDim.x) * blockDim.x) {
+    float4 pv = p[i], rv = r[i];
+    p[i] = make_float4(fmaf(b, pv.x, rv.x), fmaf(b, pv.y, rv.y), fmaf(b, pv.z, rv.z), fmaf(b, pv.w, rv.w));
+  }
+}
+
+// ---- FP64 reliable-update kernels ----
+// x += x_f ; x_f = 0
+__global__ void k_mx_accumulate(double2* __restrict__ x, float2* __restrict__ xf, long n) {
+  for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n; i += long(gridDim.x) * blockDim.x) {
+    float2 f = xf[i];
+    double2 d = x[i];
+    x[i] = make_double2(d.x + double(f.x), d.y + double(f.y));
+    xf[i] = make_float2(0.f, 0.f);
+  }
+}
+
+// r64 = b - Ax ; r = (float) r64 ; lambda = |r|^2 ; true_r2 = |r64|^2
+// mode 0: initial (p = r, delta = lambda); mode 1: reliable update
+// (beta = lambda/delta, delta = lambda, last_max = 0).
+__global__ void k_mx_residual(const double2* __restrict__ b, const double2* __restrict__ ax, double2* __restrict__ r64,
+                              float2* __restrict__ r, float2* __restrict__ p, long n, MixScal* sc, ReduceWs ws,
+                              int mode) {
+  double v[2] = {0.0, 0.0};
+  for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n; i += long(gridDim.x) * blockDim.x) {
+    double2 bb = b[i], a = ax[i];
+    double2 d = make_double2(bb.x - a.x, bb.y - a.y);
+    r64[i] = d;
+    float2 f = make_float2(float(d.x), float(d.y));
+    r[i] = f;
+    if (mode == 0) p[i] = f;
+    v[0] += double(f.x) * f.x + double(f.y) * f.y;
+    v[1] += d.x * d.x + d.y * d.y;
+  }
+  double tot[2];
+  if (grid_reduce<2>(v, ws, tot)) {
+    sc->true_r2 = tot[1];
+    sc->lambda = tot[0];
+    if (mode == 0) {
+      sc->delta = tot[0];
+      sc->beta = 0.0;
+    } else {
+      sc->beta = tot[0] / sc->delta;
+      sc->delta = tot[0];
+      sc->n_rel += 1;
+    }
+    sc->last_max = 0.0;
+    sc->need_rel = 0;
+    sc->done = (tot[0] <= sc->target2 || sc->iter >= sc->max_iter) ? 1 : 0;
+  }
+}
+
+// ---- host engine ----
+namespace {
+
+struct GraphCache {
+  cudaGraphExec_t exec = nullptr;
+  MixedBuffers key{};
+  int chunk = 0;
+  MixScal* sc = nullptr;
+};
+GraphCache g_cache;
+cudaStream_t g_cap = nullptr;
+MixScal* g_host = nullptr;
+
+bool same_key(const MixedBuffers& a, const MixedBuffers& b) {
+  return a.u32 == b.u32 && a.ph32 == b.ph32 && a.ph32_mode == b.ph32_mode && a.u32_compact == b.u32_compact &&
+         a.r == b.r && a.p == b.p && a.s == b.s && a.xf == b.xf && a.t == b.t;
+}
+
+void fp64_mdagm(const MixedBuffers& B, double2* out, const double2* in, double2* tmp, double m2, cudaStream_t st) {
+  DslashArgs<double> a;
+  a.phase_mode = PH_ANGLE;
+  a.u = B.u64;
+  a.phases = B.ph64;
+  a.stream = st;
+  a.compact_links = 0;
+  a.parity = 1; a.epilogue = EPI_PLAIN; a.out = tmp; a.in = in; a.in0 = nullptr; a.mass2 = 0;
+  launch_dslash<double>(a);
+  a.parity = 0; a.epilogue = EPI_MDAGM; a.out = out; a.in = tmp; a.in0 = in; a.mass2 = m2;
+  launch_dslash<double>(a);
+}
+
+void enqueue_iteration(const MixedBuffers& B, MixScal* sc, cudaStream_t st) {
+  const Geom& g = rt().g;
+  LinkView<float2> u{B.u32, g.sizeh, B.u32_compact ? 6 : 9};
+  const int nb = blocks_for(g.sizeh, MX_THREADS);
+  const long n4 = 3L * g.sizeh / 2;
+  int gr = reduce_grid(n4);
+  int gd = nb;
+  ReduceWs wsd = reduce_ws(1, gd > gr ? gd : gr);
+  if (B.ph32_mode == PH_SIGN8) {
+    k_mx_doe<PH_SIGN8><<<nb, MX_THREADS, 0, st>>>(g, u, B.ph32, B.p, B.t, sc);
+    k_mx_deo_dot<PH_SIGN8><<<nb, MX_THREADS, 0, st>>>(g, u, B.ph32, B.t, B.p, B.s, sc, wsd);
+  } else {
+    k_mx_doe<PH_ANGLE><<<nb, MX_THREADS, 0, st>>>(g, u, B.ph32, B.p, B.t, sc);
+    k_mx_deo_dot<PH_ANGLE><<<nb, MX_THREADS, 0, st>>>(g, u, B.ph32, B.t, B.p, B.s, sc, wsd);
+  }
+  g_kernel_launches += 2;
+  k_mx_update<<<gr, RED_THREADS, 0, st>>>(reinterpret_cast<float4*>(B.xf), reinterpret_cast<float4*>(B.r),
+                                          reinterpret_cast<const float4*>(B.p),
+                                          reinterpret_cast<const float4*>(B.s), n4, sc, wsd);
+  k_mx_pupdate<<<gr, RED_THREADS, 0, st>>>(reinterpret_cast<float4*>(B.p), reinterpret_cast<const float4*>(B.r),
+                                           n4, sc, 1);
+  g_kernel_launches += 2;
+}
+
+}  // namespace
+
+MixedResult mixed_cg(const MixedBuffers& B, const MixedOptions& o, MixScal* sc, cudaStream_t st) {
+  MixedResult res{0, 0, NAN, 0};
+  const Geom& g = rt().g;
+  const long n = 3L * g.sizeh;
+  if (!g_cap) {
+    OST_CUDA(cudaStreamCreateWithFlags(&g_cap, cudaStreamNonBlocking));
+    OST_CUDA(cudaMallocHost(&g_host, sizeof(MixScal)));
+  }
+  // order the private stream after the caller's stream
+  cudaEvent_t ev;
+  OST_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  OST_CUDA(cudaEventRecord(ev, st));
+  OST_CUDA(cudaStreamWaitEvent(g_cap, ev, 0));
+  cudaStream_t cs = g_cap;
+
+  // |b|^2 and the initial residual from the FP64 guess
+  MixScal init;
+  memset(&init, 0, sizeof(init));
+  init.m2 = o.mass2;
+  init.frac = o.delta_frac;
+  init.max_iter = o.max_iter;
+  init.every = o.reliable_every;
+  OST_CUDA(cudaMemcpyAsync(sc, &init, sizeof(MixScal), cudaMemcpyHostToDevice, cs));
+  blas_norm2<double>(B.b, n, &sc->bnorm2, cs);
+  OST_CUDA(cudaMemcpyAsync(g_host, sc, sizeof(MixScal), cudaMemcpyDeviceToHost, cs));
+  OST_CUDA(cudaStreamSynchronize(cs));
+  const double bn = g_host->bnorm2;
+  double fp32_target = o.safety * o.res;
+  init.target2 = fp32_target * fp32_target * bn;
+  init.bnorm2 = bn;
+  OST_CUDA(cudaMemcpyAsync(sc, &init, sizeof(MixScal), cudaMemcpyHostToDevice, cs));
+  blas_zero<float>(B.xf, n, cs);
+  fp64_mdagm(B, B.t64, B.x, B.t64b, o.mass2, cs);
+  {
+    int gr = reduce_grid(n);
+    k_mx_residual<<<gr, RED_THREADS, 0, cs>>>(B.b, B.t64, B.r64, B.r, B.p, n, sc, reduce_ws(2, gr), 0);
+    OST_LAUNCH_CHECK();
+  }
+
+  // workspace used inside the captured chunk is allocated before capture
+  {
+    const int nb = blocks_for(g.sizeh, MX_THREADS);
+    const int gr = reduce_grid(n);
+    reduce_ws(2, nb > gr ? nb : gr);
+  }
+  // (re)capture the iteration chunk
+  if (!g_cache.exec || !same_key(g_cache.key, B) || g_cache.chunk != o.chunk || g_cache.sc != sc) {
+    if (g_cache.exec) cudaGraphExecDestroy(g_cache.exec);
+    g_cache.exec = nullptr;
+    cudaGraph_t graph;
+    const unsigned long long counted = g_kernel_launches;   // capture launches nothing
+    OST_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+    for (int k = 0; k < o.chunk; ++k) enqueue_iteration(B, sc, cs);
+    OST_CUDA(cudaStreamEndCapture(cs, &graph));
+    g_kernel_launches = counted;
+    OST_CUDA(cudaGraphInstantiate(&g_cache.exec, graph, 0));
+    cudaGraphDestroy(graph);
+    g_cache.key = B;
+    g_cache.chunk = o.chunk;
+    g_cache.sc = sc;
+  }
+
+  const long n4 = n / 2;
+  const double res2 = o.res * o.res * bn;
+  for (int guard = 0; guard < 1000000; ++guard) {
+    if (error_code()) break;
+    OST_CUDA(cudaGraphLaunch(g_cache.exec, cs));
+    g_kernel_launches += 4ull * o.chunk;
+    OST_CUDA(cudaMemcpyAsync(g_host, sc, sizeof(MixScal), cudaMemcpyDeviceToHost, cs));
+    OST_CUDA(cudaStreamSynchronize(cs));
+    const MixScal h = *g_host;
+    if (h.need_rel) {
+      k_mx_accumulate<<<8 * rt().num_sms, 256, 0, cs>>>(B.x, B.xf, n);
+      OST_LAUNCH_CHECK();
+      fp64_mdagm(B, B.t64, B.x, B.t64b, o.mass2, cs);
+      int gr = reduce_grid(n);
+      k_mx_residual<<<gr, RED_THREADS, 0, cs>>>(B.b, B.t64, B.r64, B.r, B.p, n, sc, reduce_ws(2, gr), 1);
+      OST_LAUNCH_CHECK();
+      k_mx_pupdate<<<reduce_grid(n4), RED_THREADS, 0, cs>>>(reinterpret_cast<float4*>(B.p),
+                                                            reinterpret_cast<const float4*>(B.r), n4, sc, 0);
+      OST_LAUNCH_CHECK();
+      continue;
+    }
+    if (h.done) {
+      // fold the FP32 correction in and measure the FP64 true residual
+      k_mx_accumulate<<<8 * rt().num_sms, 256, 0, cs>>>(B.x, B.xf, n);
+      OST_LAUNCH_CHECK();
+      fp64_mdagm(B, B.t64, B.x, B.t64b, o.mass2, cs);
+      int gr = reduce_grid(n);
+      // mode 1 recomputes r, resets last_max and re-evaluates done
+      k_mx_residual<<<gr, RED_THREADS, 0, cs>>>(B.b, B.t64, B.r64, B.r, B.p, n, sc, reduce_ws(2, gr), 1);
+      OST_LAUNCH_CHECK();
+      OST_CUDA(cudaMemcpyAsync(g_host, sc, sizeof(MixScal), cudaMemcpyDeviceToHost, cs));
+      OST_CUDA(cudaStreamSynchronize(cs));
+      const MixScal f = *g_host;
+      res.iters = f.iter;
+      res.n_reliable = f.n_rel - 1;   // the closing residual is not an update
+      res.true_res = std::sqrt(f.true_r2 / bn);
+      res.converged = f.true_r2 <= res2;
+      if (res.converged || !o.guarantee || f.iter >= o.max_iter) break;
+      // not there yet in FP64: tighten the FP32 target and continue from the
+      // recomputed residual (the closing residual acts as a reliable update)
+      fp32_target *= 0.5;
+      MixScal upd = f;
+      upd.target2 = fp32_target * fp32_target * bn;
+      upd.done = (f.lambda <= upd.target2) ? 1 : 0;
+      OST_CUDA(cudaMemcpyAsync(sc, &upd, sizeof(MixScal), cudaMemcpyHostToDevice, cs));
+      k_mx_pupdate<<<reduce_grid(n4), RED_THREADS, 0, cs>>>(reinterpret_cast<float4*>(B.p),
+                                                            reinterpret_cast<const float4*>(B.r), n4, sc, 0);
+      OST_LAUNCH_CHECK();
+      continue;
+    }
+  }
+  OST_CUDA(cudaEventRecord(ev, cs));
+  OST_CUDA(cudaStreamWaitEvent(st, ev, 0));
+  OST_CUDA(cudaEventDestroy(ev));
+  return res;
+}
+
+// Times `reps` launches of one FP32 solver kernel on stream st with CUDA
+// events recorded on that stream; returns the mean milliseconds per launch.
+// which = 1: D_oe (t = D_oe p); which = 2: fused D_eo + M^+M epilogue + dot.
+double time_mixed_kernel(const MixedBuffers& B, MixScal* sc, int which, int reps, cudaStream_t st) {
+  const Geom& g = rt().g;
+  LinkView<float2> u{B.u32, g.sizeh, B.u32_compact ? 6 : 9};
+  const int nb = blocks_for(g.sizeh, MX_THREADS);
+  MixScal init;
+  memset(&init, 0, sizeof(init));
+  init.m2 = 0.01;
+  init.delta = 1.0;
+  OST_CUDA(cudaMemcpyAsync(sc, &init, sizeof(MixScal), cudaMemcpyHostToDevice, st));
+  ReduceWs ws = reduce_ws(1, nb);
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float ms = 0;
+  for (int pass = 0; pass < 2; ++pass) {       // pass 0 warms up
+    cudaEventRecord(e0, st);
+    for (int k = 0; k < reps; ++k) {
+      if (which == 1) {
+        if (B.ph32_mode == PH_SIGN8) k_mx_doe<PH_SIGN8><<<nb, MX_THREADS, 0, st>>>(g, u, B.ph32, B.p, B.t, sc);
+        else k_mx_doe<PH_ANGLE><<<nb, MX_THREADS, 0, st>>>(g, u, B.ph32, B.p, B.t, sc);
+      } else {
+        if (B.ph32_mode == PH_SIGN8)
+          k_mx_deo_dot<PH_SIGN8><<<nb, MX_THREADS, 0, st>>>(g, u, B.ph32, B.t, B.p, B.s, sc, ws);
+        else k_mx_deo_dot<PH_ANGLE><<<nb, MX_THREADS, 0, st>>>(g, u, B.ph32, B.t, B.p, B.s, sc, ws);
+      }
+      OST_LAUNCH_CHECK();
+    }
+    cudaEventRecord(e1, st);
+    cudaEventSynchronize(e1);
+    cudaEventElapsedTime(&ms, e0, e1);
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return double(ms) / reps;
+}
+
+}  // namespace ost

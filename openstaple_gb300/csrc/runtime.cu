@@ -15,6 +15,7 @@
 namespace ost {
 
 static Runtime g_rt;
+unsigned long long g_kernel_launches = 0;
 Runtime& rt() { return g_rt; }
 
 static int g_err = 0;
@@ -242,6 +243,24 @@ int ostaple_update_host(void* host, size_t bytes) {
                            cudaMemcpyDeviceToHost, g_rt.stream));
   OST_CUDA(cudaStreamSynchronize(g_rt.stream));
   return g_err;
+}
+
+unsigned long long ostaple_kernel_launches(void) { return g_kernel_launches; }
+
+int ostaple_pin_host(void* host, size_t bytes) {
+  cudaError_t e = cudaHostRegister(host, bytes, cudaHostRegisterDefault);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    set_error(int(e), "ostaple_pin_host: %s", cudaGetErrorString(e));
+    return int(e);
+  }
+  return 0;
+}
+
+int ostaple_unpin_host(void* host) {
+  cudaError_t e = cudaHostUnregister(host);
+  if (e != cudaSuccess) { cudaGetLastError(); return int(e); }
+  return 0;
 }
 
 void* ostaple_deviceptr(const void* host) {

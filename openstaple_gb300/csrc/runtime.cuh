@@ -36,7 +36,14 @@ void clear_error();
     }                                                                        \
   } while (0)
 
-#define OST_LAUNCH_CHECK() OST_CUDA(cudaGetLastError())
+// Every kernel launch of the library goes through OST_LAUNCH_CHECK, which
+// also counts it (graph replays add the kernels they contain).
+extern unsigned long long g_kernel_launches;
+#define OST_LAUNCH_CHECK()          \
+  do {                              \
+    ++::ost::g_kernel_launches;     \
+    OST_CUDA(cudaGetLastError());   \
+  } while (0)
 
 bool require_init(const char* who);
 

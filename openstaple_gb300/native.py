@@ -98,6 +98,10 @@ SIGNATURES = {
     "ostaple_update_host": (_I, [_P, C.c_size_t]),
     "ostaple_deviceptr": (_P, [_P]),
     "ostaple_probe_fma_tflops": (_I, [_I, C.POINTER(_D)]),
+    "ostaple_kernel_launches": (C.c_ulonglong, []),
+    "ostaple_pin_host": (_I, [_P, C.c_size_t]),
+    "ostaple_unpin_host": (_I, [_P]),
+    "ostaple_time_kernel": (_I, [_I, _P, _P, _I, C.POINTER(_D)]),
     "acc_Deo": (None, [_P, _P, _P, _P]),
     "acc_Doe": (None, [_P, _P, _P, _P]),
     "acc_Deo_unsafe": (None, [_P, _P, _P, _P]),
@@ -125,6 +129,11 @@ SIGNATURES = {
     "multishift_invert": (_I, [_P, C.POINTER(FermParam), C.POINTER(RationalApprox), _P, _P, _D, _P, _P, _P, _P,
                                _P, _I, C.POINTER(_I)]),
     "recombine_shifted_vec3_to_vec3": (None, [_P, _P, _P, C.POINTER(RationalApprox)]),
+    "inverter_mixed_precision": (_I, [InverterPackage, C.POINTER(FermParam), _P, _P, _D, _I, _D, C.POINTER(_I)]),
+    "inverter_wrapper": (_I, [InverterPackage, C.POINTER(FermParam), _P, _P, _D, _I, _D, _I]),
+    "convergence_messages": (None, [_I, _I]),
+    "ostaple_invert_mixed": (_I, [_P, _P, _D, _D, _P, _P, _D, _I, _I, C.POINTER(_I), C.POINTER(_D),
+                                  C.POINTER(_I)]),
 }
 
 _lib = None
@@ -137,7 +146,7 @@ def lib() -> C.CDLL:
         if not LIB_PATH.exists():
             raise RuntimeError(
                 f"{LIB_PATH} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`")
-        L = C.CDLL(str(LIB_PATH), mode=C.RTLD_GLOBAL)
+        L = C.CDLL(str(LIB_PATH), mode=C.RTLD_LOCAL)
         for name, (res, args) in SIGNATURES.items():
             f = getattr(L, name)
             f.restype = res

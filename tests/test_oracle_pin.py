@@ -77,8 +77,9 @@ def test_oracle_matches_compiled_reference(built, dims):
     assert np.array_equal(o.phases(), ph)
     u = F.random_su3_links(dims, 101)
     v = F.gaussian_vec3(dims, 102)
-    assert np.array_equal(o.Deo(u, v, ph), r.Deo(u, v, ph))
-    assert np.array_equal(o.Doe(u, v, ph), r.Doe(u, v, ph))
+    # same arithmetic up to the compiler's FMA contraction choices
+    assert relerr(o.Deo(u, v, ph), r.Deo(u, v, ph)) <= 2e-16
+    assert relerr(o.Doe(u, v, ph), r.Doe(u, v, ph)) <= 2e-16
     # a generic (imaginary chemical potential) phase exercises the cos/sin path
     ph2 = r.phases(0.3)
     assert np.array_equal(o.phases(0.3), ph2)
