@@ -58,6 +58,8 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--skip-fp64", action="store_true", help="skip the plain FP64 CG arm (profiling runs)")
+    ap.add_argument("--delta", type=float, default=0.1,
+                    help="reliable update when |r|^2 < delta * max|r|^2 since the last one")
     return ap.parse_args()
 
 
@@ -84,7 +86,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
         except (OSError, FileNotFoundError):
@@ -234,15 +236,14 @@ def main():
 
     def solve():
         L.set_vec3_soa_to_zero(x.ctypes.data)
-        return api.invert_mixed(u, ph, args.mass, 0.0, x, b, args.res, 100000, 0)
+        return api.invert_mixed(u, ph, args.mass, 0.0, x, b, args.res, 100000, 0, args.delta)
 
-    for _ in range(args.warmup):
-        info = solve()
-    barrier()
-    launches0 = L.ostaple_kernel_launches()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clk:
+        for _ in range(args.warmup):
+            info = solve()
         barrier()
+        launches0 = L.ostaple_kernel_launches()
         e0.record(stream)
         infos = [solve() for _ in range(args.steps)]
         e1.record(stream)
@@ -287,7 +288,7 @@ def main():
             t0 = time.perf_counter()
             for a in (u, ph, b, x):
                 lat.update_device(a)
-            api.invert_mixed(u, ph, args.mass, 0.0, x, b, args.res, 100000, 0)
+            api.invert_mixed(u, ph, args.mass, 0.0, x, b, args.res, 100000, 0, args.delta)
             lat.update_host(x)
             dt = time.perf_counter() - t0
             if k >= args.warmup:

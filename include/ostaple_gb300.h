@@ -115,6 +115,26 @@ typedef struct inverter_package_t {       /* OpenAcc/inverter_package.h:13-31 */
 } inverter_package;
 #endif
 
+#ifndef OSTAPLE_HAVE_REFERENCE_TYPES
+typedef struct action_param_t {           /* OpenAcc/action.h:8-20 */
+  double beta;
+  int stout_steps;
+  double stout_rho;
+  int topo_action;
+  double barrier;
+  double width;
+  char topo_file_path[20];
+  int topo_stout_steps;
+  double topo_rho;
+} action_param;
+#endif
+
+/* Stout parameters read by stout_wrapper / fermion_force_soloopenacc and the
+ * stout kernels (action.h:22-23).  Weak library defaults: 2 steps of
+ * rho = 0.15; a host definition overrides them. */
+extern action_param act_params;
+extern double gl_stout_rho, gl_topo_rho;
+
 /* Inverter switches read by the dispatch wrappers.  The reference host
  * defines this global (Include/inverter_tricks.c); the library carries a
  * weak default {0, 0, 0.1, 10000} that a host definition overrides. */
@@ -244,15 +264,58 @@ void convergence_messages(int conv_importance, int inverter_status);
 int inverter_wrapper(inverter_package ip, ferm_param *pars, vec3_soa *out, const vec3_soa *in, double res,
                      int max_cg, double shift, int convergence_importance);
 
+/* ---- stout smearing (stouting.h:13-44) ---------------------------------- */
+/* U' = exp(-Q_A) U with Q_A = rho/C_0 TA(U C), C the tree-level-Symanzik
+ * weighted staples; writes uprime (rows 0,1), local_staples (if not NULL)
+ * and tipdot = Q_A; rho = gl_stout_rho (gl_topo_rho if istopo). */
+void stout_isotropic(const su3_soa *u, su3_soa *uprime, su3_soa *local_staples, su3_soa *auxiliary,
+                     tamat_soa *tipdot, const int istopo);
+/* act_params.stout_steps levels into tstout_conf_acc_arr[8*level] (stouting.c:27-72) */
+void stout_wrapper(const su3_soa *tconf_acc, su3_soa *tstout_conf_acc_arr, const int istopo);
+/* tu_out = exp(-QA) tu (stouting.c:136-165) */
+void exp_minus_QA_times_conf(const su3_soa *tu, const tamat_soa *QA, su3_soa *tu_out, su3_soa *exp_aux);
+/* Lambda of the stout chain rule (stouting.c:516-546) */
+void compute_lambda(thmat_soa *L, const su3_soa *SP, const su3_soa *U, const tamat_soa *QA, su3_soa *TMP);
+/* S: Sigma' in, Sigma out (stouting.c:1175-1302) */
+void compute_sigma(const thmat_soa *L, const su3_soa *U, su3_soa *S, const tamat_soa *QA, su3_soa *TMP,
+                   const int istopo);
+/* staples, Q_A, Lambda and Sigma for one level (fermion_force.c:52-162) */
+void compute_sigma_from_sigma_prime_backinto_sigma_prime(su3_soa *Sigma, thmat_soa *Lambda, tamat_soa *QA,
+                                                         const su3_soa *U, su3_soa *TMP, const int istopo);
+void set_su3_soa_to_zero(su3_soa *matrix);                    /* su3_utilities.c:43-55 */
+void set_tamat_soa_to_zero(tamat_soa *matrix);                /* fermion_force_utilities.c:16-28 */
+
+/* ---- rational fermion force (fermion_force_utilities.h:204-240) ---------- */
+/* aux_u += RA_a[iter] (D_oe X)(x+mu) (x) X(x)^+ on even, the mirror on odd links */
+void direct_product_of_fermions_into_auxmat(const vec3_soa *loc_s, const vec3_soa *loc_h, su3_soa *aux_u,
+                                            const RationalApprox *approx, int iter);
+/* the outer products of all approx_md shifts (fermion_force_utilities.c:183-201) */
+void ker_openacc_compute_fermion_force(const su3_soa *u, su3_soa *aux_u, const vec3_soa *in_shiftmulti,
+                                       vec3_soa *loc_s, vec3_soa *loc_h, ferm_param *tpars);
+/* pseudo_ipdot += e^{i theta} auxmat (fermion_force_utilities.c:123-153) */
+void multiply_backfield_times_force(ferm_param *tpars, const su3_soa *auxmat, su3_soa *pseudo_ipdot);
+/* ipdot -= TA(U auxmat) (fermion_force_utilities.c:95-121) */
+void multiply_conf_times_force_and_take_ta_nophase(const su3_soa *u, const su3_soa *auxmat, tamat_soa *ipdot);
+/* the whole force of all flavours through the stout levels (fermion_force.h:23-36) */
+void fermion_force_soloopenacc(su3_soa *tconf_acc, su3_soa *tstout_conf_acc_arr, su3_soa *gl3_aux,
+                               tamat_soa *tipdot_acc, ferm_param *tfermion_parameters, int tNDiffFlavs,
+                               const vec3_soa *ferm_in_acc, double res, su3_soa *taux_conf_acc,
+                               vec3_soa *tferm_shiftmulti_acc, inverter_package ipt, const int max_cg);
+/* multi-shift dispatch; with inverter_tricks.singlePInvAccelMultiInv every
+ * shift is then refined by inverter_wrapper (inverter_wrappers.c:41-114) */
+int inverter_multishift_wrapper(inverter_package ip, ferm_param *pars, RationalApprox *approx, vec3_soa *out,
+                                const vec3_soa *in, double res, int max_cg, int convergence_importance);
+
 /* Mixed-precision CG that iterates until the FP64 true residual
  * sqrt(|b - (M^+M + shift) x|^2 / |b|^2) is <= res (or max_iter), with a
- * reliable update every `reliable_every` iterations (0: the reference's
- * delta criterion).  Reports iterations, the final FP64 true residual and
- * the number of reliable updates.  Extends inverter_mixed_precision; no
- * reference counterpart. */
+ * reliable update every `reliable_every` iterations, or (reliable_every = 0)
+ * when |r|^2 < delta_frac * max|r|^2 since the last one (delta_frac <= 0:
+ * inverter_tricks.mixedPrecisionDelta).  Reports iterations, the final FP64
+ * true residual and the number of reliable updates.  Extends
+ * inverter_mixed_precision; no reference counterpart. */
 int ostaple_invert_mixed(const su3_soa *u, const double_soa *phases, double mass, double shift,
                          vec3_soa *solution, const vec3_soa *in, double res, int max_iter, int reliable_every,
-                         int *iters, double *true_res, int *n_reliable);
+                         double delta_frac, int *iters, double *true_res, int *n_reliable);
 
 #ifdef __cplusplus
 }

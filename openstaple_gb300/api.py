@@ -193,10 +193,54 @@ def inverter_mixed_precision(ip: InverterPackage, pars: FermParam, solution, inp
 
 
 def invert_mixed(u, phases, mass: float, shift: float, solution, inp, res: float = 1e-10, max_iter: int = 100000,
-                 reliable_every: int = 0) -> dict:
+                 reliable_every: int = 0, delta_frac: float = 0.0) -> dict:
     """Mixed-precision solve to an FP64 true residual <= res."""
     it, nrel, tr = C.c_int(0), C.c_int(0), C.c_double(0)
     st = lib().ostaple_invert_mixed(ptr(u), ptr(phases), mass, shift, ptr(solution), ptr(inp), res, max_iter,
-                                    reliable_every, C.byref(it), C.byref(tr), C.byref(nrel))
+                                    reliable_every, delta_frac, C.byref(it), C.byref(tr), C.byref(nrel))
     check(0, "ostaple_invert_mixed")
     return dict(status=st, iters=it.value, true_res=tr.value, n_reliable=nrel.value)
+
+
+# ---- stout smearing and fermion force (stouting.h, fermion_force_utilities.h) ----
+def su3_field(sizeh: int, n: int = 8) -> np.ndarray:
+    """su3_soa[n] in the reference layout: complex128 (n, 3, 3, sizeh)."""
+    return np.zeros((n, 3, 3, sizeh), np.complex128)
+
+
+def alg_field(sizeh: int) -> np.ndarray:
+    """tamat_soa[8] / thmat_soa[8]: float64 (8, 8*sizeh) (3 complex + 2 real arrays per direction)."""
+    return np.zeros((8, 8 * sizeh))
+
+
+def stout_isotropic(u, uprime, local_staples, auxiliary, tipdot, istopo: int = 0) -> None:
+    lib().stout_isotropic(ptr(u), ptr(uprime), None if local_staples is None else ptr(local_staples),
+                          None if auxiliary is None else ptr(auxiliary), ptr(tipdot), istopo)
+    check(0, "stout_isotropic")
+
+
+def stout_wrapper(u, stout_levels, istopo: int = 0) -> None:
+    lib().stout_wrapper(ptr(u), ptr(stout_levels), istopo)
+    check(0, "stout_wrapper")
+
+
+def compute_sigma_from_sigma_prime_backinto_sigma_prime(sigma, lam, qa, u, tmp, istopo: int = 0) -> None:
+    lib().compute_sigma_from_sigma_prime_backinto_sigma_prime(ptr(sigma), ptr(lam), ptr(qa), ptr(u), ptr(tmp),
+                                                              istopo)
+    check(0, "compute_sigma_from_sigma_prime_backinto_sigma_prime")
+
+
+def ker_openacc_compute_fermion_force(u, aux_u, in_shiftmulti, loc_s, loc_h, pars: FermParam) -> None:
+    lib().ker_openacc_compute_fermion_force(ptr(u), ptr(aux_u), ptr(in_shiftmulti), ptr(loc_s), ptr(loc_h),
+                                            C.byref(pars))
+    check(0, "ker_openacc_compute_fermion_force")
+
+
+def multiply_backfield_times_force(pars: FermParam, auxmat, pseudo_ipdot) -> None:
+    lib().multiply_backfield_times_force(C.byref(pars), ptr(auxmat), ptr(pseudo_ipdot))
+    check(0, "multiply_backfield_times_force")
+
+
+def multiply_conf_times_force_and_take_ta_nophase(u, auxmat, ipdot) -> None:
+    lib().multiply_conf_times_force_and_take_ta_nophase(ptr(u), ptr(auxmat), ptr(ipdot))
+    check(0, "multiply_conf_times_force_and_take_ta_nophase")

@@ -123,8 +123,8 @@ int inverter_mixed_precision(inverter_package ip, ferm_param* pars, vec3_soa* so
 }
 
 int ostaple_invert_mixed(const su3_soa* u, const double_soa* phases, double mass, double shift, vec3_soa* solution,
-                         const vec3_soa* in, double res, int max_iter, int reliable_every, int* iters,
-                         double* true_res, int* n_reliable) {
+                         const vec3_soa* in, double res, int max_iter, int reliable_every, double delta_frac,
+                         int* iters, double* true_res, int* n_reliable) {
   if (!require_init("ostaple_invert_mixed")) return INVERTER_FAILURE;
   cudaStream_t st = rt().stream;
   MixedBuffers B{};
@@ -154,7 +154,7 @@ int ostaple_invert_mixed(const su3_soa* u, const double_soa* phases, double mass
   o.safety = 0.9;
   o.max_iter = max_iter;
   o.reliable_every = reliable_every;
-  o.delta_frac = inverter_tricks.mixedPrecisionDelta;
+  o.delta_frac = delta_frac > 0 ? delta_frac : inverter_tricks.mixedPrecisionDelta;
   o.guarantee = 1;
   o.chunk = 8;
   MixScal* sc = mix_scalars();

@@ -86,7 +86,7 @@ k_mx_deo_dot(Geom g, LinkView<float2> u, const void* __restrict__ ph, const floa
              const float2* __restrict__ p, float2* __restrict__ s, MixScal* sc, ReduceWs ws) {
   if (halted(sc)) return;
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  double v[1] = {0.0};
+  float v[1] = {0.0f};
   if (idx < g.sizeh) {
     const float m2 = float(sc->m2);
     float2 aux[3];
@@ -97,11 +97,11 @@ k_mx_deo_dot(Geom g, LinkView<float2> u, const void* __restrict__ ph, const floa
       float2 pv = p[k];
       float2 r = make_float2(fmaf(pv.x, m2, -0.5f * aux[c].x), fmaf(pv.y, m2, -0.5f * aux[c].y));
       s[k] = r;
-      v[0] += double(pv.x) * double(r.x) + double(pv.y) * double(r.y);
+      v[0] = fmaf(pv.x, r.x, fmaf(pv.y, r.y, v[0]));
     }
   }
   double tot[1];
-  if (grid_reduce<1>(v, ws, tot)) {
+  if (grid_reduce_f32w<1>(v, ws, tot)) {
     sc->pAp = tot[0];
     sc->alpha = sc->delta / tot[0];
   }
@@ -116,7 +116,7 @@ __global__ void k_mx_update(float4* __restrict__ xf, float4* __restrict__ r, con
   const double lm = sc->last_max > delta ? sc->last_max : delta;
   const bool rel = sc->every > 0 ? ((sc->iter + 1) % sc->every == 0) : (delta < sc->frac * lm);
   const float a = float(sc->alpha);
-  double v[1] = {0.0};
+  float v[1] = {0.0f};
   for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n4; i += long(gridDim.x) * blockDim.x) {
     float4 pv = p[i], xv = xf[i];
     xv.x = fmaf(a, pv.x, xv.x); xv.y = fmaf(a, pv.y, xv.y); xv.z = fmaf(a, pv.z, xv.z); xv.w = fmaf(a, pv.w, xv.w);
@@ -125,11 +125,11 @@ __global__ void k_mx_update(float4* __restrict__ xf, float4* __restrict__ r, con
       float4 sv = s[i], rv = r[i];
       rv.x = fmaf(-a, sv.x, rv.x); rv.y = fmaf(-a, sv.y, rv.y); rv.z = fmaf(-a, sv.z, rv.z); rv.w = fmaf(-a, sv.w, rv.w);
       r[i] = rv;
-      v[0] += double(rv.x) * rv.x + double(rv.y) * rv.y + double(rv.z) * rv.z + double(rv.w) * rv.w;
+      v[0] = fmaf(rv.x, rv.x, fmaf(rv.y, rv.y, fmaf(rv.z, rv.z, fmaf(rv.w, rv.w, v[0]))));
     }
   }
   double tot[1];
-  if (grid_reduce<1>(v, ws, tot)) {
+  if (grid_reduce_f32w<1>(v, ws, tot)) {
     sc->iter += 1;
     sc->last_max = lm;
     if (rel) {

@@ -90,4 +90,57 @@ OST_D bool grid_reduce(double v[NV], ReduceWs ws, double tot[NV]) {
   return false;
 }
 
+// Variant for single-precision solvers: per-thread values and the
+// intra-warp tree in FP32 (GB300 runs FP64 at 1/64 of the FP32 rate, so FP64
+// per-thread accumulation would cost as much as the memory traffic), the
+// cross-warp and cross-block sums in FP64.  Same fixed order, so results
+// stay bitwise reproducible.
+template <int NV>
+OST_D bool grid_reduce_f32w(float vf[NV], ReduceWs ws, double tot[NV]) {
+  __shared__ double smem[NV * 32];
+  __shared__ bool am_last;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nwarps = (blockDim.x + 31) >> 5;
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) vf[k] += __shfl_down_sync(0xffffffffu, vf[k], o);
+  }
+  if (lane == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) smem[k * 32 + warp] = double(vf[k]);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      double t = 0.0;
+      for (int w = 0; w < nwarps; ++w) t += smem[k * 32 + w];
+      ws.partials[k * ws.max_blocks + blockIdx.x] = t;
+    }
+    __threadfence();
+    unsigned int t = atomicAdd(ws.counter, 1u);
+    am_last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!am_last) return false;
+  __threadfence();
+  double s[NV];
+#pragma unroll
+  for (int k = 0; k < NV; ++k) s[k] = 0.0;
+  for (int b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) s[k] += __ldcg(ws.partials + k * ws.max_blocks + b);
+  }
+  __syncthreads();
+  block_reduce<NV>(s, smem);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) tot[k] = s[k];
+    *ws.counter = 0;
+    return true;
+  }
+  return false;
+}
+
 }  // namespace ost

@@ -132,8 +132,24 @@ SIGNATURES = {
     "inverter_mixed_precision": (_I, [InverterPackage, C.POINTER(FermParam), _P, _P, _D, _I, _D, C.POINTER(_I)]),
     "inverter_wrapper": (_I, [InverterPackage, C.POINTER(FermParam), _P, _P, _D, _I, _D, _I]),
     "convergence_messages": (None, [_I, _I]),
-    "ostaple_invert_mixed": (_I, [_P, _P, _D, _D, _P, _P, _D, _I, _I, C.POINTER(_I), C.POINTER(_D),
+    "ostaple_invert_mixed": (_I, [_P, _P, _D, _D, _P, _P, _D, _I, _I, _D, C.POINTER(_I), C.POINTER(_D),
                                   C.POINTER(_I)]),
+    "stout_isotropic": (None, [_P, _P, _P, _P, _P, _I]),
+    "stout_wrapper": (None, [_P, _P, _I]),
+    "exp_minus_QA_times_conf": (None, [_P, _P, _P, _P]),
+    "compute_lambda": (None, [_P, _P, _P, _P, _P]),
+    "compute_sigma": (None, [_P, _P, _P, _P, _P, _I]),
+    "compute_sigma_from_sigma_prime_backinto_sigma_prime": (None, [_P, _P, _P, _P, _P, _I]),
+    "set_su3_soa_to_zero": (None, [_P]),
+    "set_tamat_soa_to_zero": (None, [_P]),
+    "direct_product_of_fermions_into_auxmat": (None, [_P, _P, _P, C.POINTER(RationalApprox), _I]),
+    "ker_openacc_compute_fermion_force": (None, [_P, _P, _P, _P, _P, C.POINTER(FermParam)]),
+    "multiply_backfield_times_force": (None, [C.POINTER(FermParam), _P, _P]),
+    "multiply_conf_times_force_and_take_ta_nophase": (None, [_P, _P, _P]),
+    "fermion_force_soloopenacc": (None, [_P, _P, _P, _P, C.POINTER(FermParam), _I, _P, _D, _P, _P,
+                                         InverterPackage, _I]),
+    "inverter_multishift_wrapper": (_I, [InverterPackage, C.POINTER(FermParam), C.POINTER(RationalApprox), _P, _P,
+                                         _D, _I, _I]),
 }
 
 _lib = None
@@ -153,6 +169,24 @@ def lib() -> C.CDLL:
             f.argtypes = args
         _lib = L
     return _lib
+
+
+class ActionParam(C.Structure):
+    """Layout of the reference's action_param (OpenAcc/action.h:8-20)."""
+    _fields_ = [
+        ("beta", C.c_double), ("stout_steps", C.c_int), ("stout_rho", C.c_double), ("topo_action", C.c_int),
+        ("barrier", C.c_double), ("width", C.c_double), ("topo_file_path", C.c_char * 20),
+        ("topo_stout_steps", C.c_int), ("topo_rho", C.c_double),
+    ]
+
+
+def act_params() -> ActionParam:
+    """The library's `act_params` global (writable)."""
+    return ActionParam.in_dll(lib(), "act_params")
+
+
+def set_stout_rho(rho: float) -> None:
+    C.c_double.in_dll(lib(), "gl_stout_rho").value = float(rho)
 
 
 def inverter_tricks() -> InvTricks:

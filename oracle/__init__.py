@@ -43,6 +43,16 @@ class Oracle:
         "orc_cg": (_I, [_P, _P, _D, _P, _P, _D, _I, _D, _I, C.POINTER(_I)]),
         "orc_cgm": (_I, [_P, _P, _D, _I, _P, _P, _P, _D, _I, C.POINTER(_I)]),
         "orc_recombine": (None, [_P, _P, _P, _I, _D, _P]),
+        "orc_staples": (None, [_P, _P]),
+        "orc_rho_ta": (None, [_P, _P, _P, _D]),
+        "orc_exp_times_conf": (None, [_P, _P, _P]),
+        "orc_stout": (None, [_P, _P, _D]),
+        "orc_lambda": (None, [_P, _P, _P, _P]),
+        "orc_sigma": (None, [_P, _P, _P, _P, _D]),
+        "orc_sigma_prime_to_sigma": (None, [_P, _P, _D]),
+        "orc_force_outer": (None, [_P, _P, _P, _P, _I, _P]),
+        "orc_backfield_times_force": (None, [_P, _P, _P]),
+        "orc_conf_times_force_ta": (None, [_P, _P, _P]),
     }
 
     def __init__(self, dims, threads: int = 1):
@@ -101,6 +111,54 @@ class Oracle:
         a = np.ascontiguousarray(a, dtype=np.float64)
         out = np.zeros((3, self.sizeh), np.complex128)
         self.L.orc_recombine(_p(xs), _p(b), _p(out), len(a), a0, _p(a))
+        return out
+
+    # --- gauge part: su3[8] = complex (8,3,3,sizeh); tamat/thmat = float (8, 8*sizeh) ---
+    def su3(self):
+        return np.zeros((8, 3, 3, self.sizeh), np.complex128)
+
+    def tamat(self):
+        return np.zeros((8, 8 * self.sizeh))
+
+    def staples(self, u):
+        s = self.su3()
+        self.L.orc_staples(_p(u), _p(s))
+        return s
+
+    def rho_ta(self, u, stap, rho):
+        q = self.tamat()
+        self.L.orc_rho_ta(_p(u), _p(stap), _p(q), rho)
+        return q
+
+    def stout(self, u, rho):
+        out = u.copy()
+        self.L.orc_stout(_p(u), _p(out), rho)
+        return out
+
+    def sigma_prime_to_sigma(self, sigma, u, rho):
+        s = sigma.copy()
+        self.L.orc_sigma_prime_to_sigma(_p(s), _p(u), rho)
+        return s
+
+    def lambda_(self, sp, u, qa):
+        lam = self.tamat()
+        self.L.orc_lambda(_p(lam), _p(sp), _p(u), _p(qa))
+        return lam
+
+    def force_outer(self, u, xs, ph, a):
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        aux = self.su3()
+        self.L.orc_force_outer(_p(u), _p(aux), _p(xs), _p(ph), len(a), _p(a))
+        return aux
+
+    def backfield_times_force(self, ph, aux, pip):
+        out = pip.copy()
+        self.L.orc_backfield_times_force(_p(ph), _p(aux), _p(out))
+        return out
+
+    def conf_times_force_ta(self, u, sigma, ipdot):
+        out = ipdot.copy()
+        self.L.orc_conf_times_force_ta(_p(u), _p(sigma), _p(out))
         return out
 
 
@@ -190,4 +248,46 @@ class Reference:
         a = np.ascontiguousarray(a, dtype=np.float64)
         out = np.zeros((3, self.sizeh), np.complex128)
         self.L.ref_recombine(_p(xs), _p(b), _p(out), len(a), a0, _p(a))
+        return out
+
+    def su3(self):
+        return np.zeros((8, 3, 3, self.sizeh), np.complex128)
+
+    def tamat(self):
+        return np.zeros((8, 8 * self.sizeh))
+
+    def staples(self, u):
+        s = self.su3()
+        self.L.ref_staples(_p(u), _p(s))
+        return s
+
+    def rho_ta(self, u, stap, rho):
+        q = self.tamat()
+        self.L.ref_rho_ta(_p(u), _p(stap), _p(q), rho)
+        return q
+
+    def stout(self, u, rho):
+        out = u.copy()
+        self.L.ref_stout_isotropic(_p(u), _p(out), rho)
+        return out
+
+    def sigma_prime_to_sigma(self, sigma, u, rho):
+        s = sigma.copy()
+        self.L.ref_sigma_prime_to_sigma(_p(s), _p(u), rho)
+        return s
+
+    def force_outer(self, u, xs, ph, a):
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        aux = self.su3()
+        self.L.ref_force_outer_products(_p(u), _p(aux), _p(xs), _p(ph), 0.0, len(a), _p(a))
+        return aux
+
+    def backfield_times_force(self, ph, aux, pip):
+        out = pip.copy()
+        self.L.ref_backfield_times_force(_p(ph), _p(aux), _p(out))
+        return out
+
+    def conf_times_force_ta(self, u, sigma, ipdot):
+        out = ipdot.copy()
+        self.L.ref_conf_times_force_ta(_p(u), _p(sigma), _p(out))
         return out

@@ -25,6 +25,7 @@ int orc_init(int n0, int n1, int n2, int n3)
   N[0] = n0; N[1] = n1; N[2] = n2; N[3] = n3;
   VL[0] = 1; VL[1] = n0; VL[2] = (long)n0 * n1; VL[3] = (long)n0 * n1 * n2;
   SH = (long)n0 * n1 * n2 * n3 / 2;
+  orc_gauge_init(n0, n1, n2, n3);
   return (int)SH;
 }
 

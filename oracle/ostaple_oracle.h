@@ -40,4 +40,17 @@ int orc_cgm(const ocplx *u, const double *ph, double mass, int order, const doub
             const ocplx *b, double res, int max_cg, int *cg_out);
 void orc_recombine(const ocplx *xs, const ocplx *b, ocplx *out, int order, double a0, const double *a);
 
+/* stout smearing and force chain (ostaple_oracle_gauge.c) */
+void orc_gauge_init(int n0, int n1, int n2, int n3);
+void orc_staples(const ocplx *u, ocplx *stap);
+void orc_rho_ta(const ocplx *u, const ocplx *stap, double *qa, double rho);
+void orc_exp_times_conf(const ocplx *u, double *qa, ocplx *uout);
+void orc_stout(const ocplx *u, ocplx *uout, double rho);
+void orc_lambda(double *lam, const ocplx *sp, const ocplx *u, double *qa);
+void orc_sigma(double *lam, const ocplx *u, ocplx *s, double *qa, double rho);
+void orc_sigma_prime_to_sigma(ocplx *sigma, const ocplx *u, double rho);
+void orc_force_outer(const ocplx *u, ocplx *aux, const ocplx *xs, const double *ph, int order, const double *a);
+void orc_backfield_times_force(const double *ph, const ocplx *aux, ocplx *pip);
+void orc_conf_times_force_ta(const ocplx *u, const ocplx *sigma, double *ipdot);
+
 #endif
