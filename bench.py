@@ -58,7 +58,7 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--skip-fp64", action="store_true", help="skip the plain FP64 CG arm (profiling runs)")
-    ap.add_argument("--delta", type=float, default=0.1,
+    ap.add_argument("--delta", type=float, default=1e-4,
                     help="reliable update when |r|^2 < delta * max|r|^2 since the last one")
     return ap.parse_args()
 

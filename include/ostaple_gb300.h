@@ -317,6 +317,25 @@ int ostaple_invert_mixed(const su3_soa *u, const double_soa *phases, double mass
                          vec3_soa *solution, const vec3_soa *in, double res, int max_iter, int reliable_every,
                          double delta_frac, int *iters, double *true_res, int *n_reliable);
 
+/* ---- batched solvers (no reference counterpart: the reference solves one
+ * right-hand side at a time, update_versatile.c:258-275) --------------------- */
+/* nsys solves (M^+M + shifts[k]) x_k = b_k sharing the links: every FP32
+ * Dslash reads each link once for a batch of up to 8 systems; each system
+ * keeps its own scalars and reliable updates and reaches its own FP64 true
+ * residual <= res.  solutions/sources: nsys consecutive vec3_soa; shifts may
+ * be NULL (all zero).  delta_frac <= 0 selects 1e-4. */
+int ostaple_invert_mixed_batch(const su3_soa *u, const double_soa *phases, double mass, int nsys,
+                               const double *shifts, vec3_soa *solutions, const vec3_soa *sources, double res,
+                               int max_iter, double delta_frac, int *iters, double *true_res, int *n_reliable);
+/* all shifts of approx for nrhs (1..4) right-hand sides: an FP32 multi-shift
+ * CG for all right-hand sides together, then every (rhs, shift) system refined
+ * by the batched mixed solver to an FP64 true residual <= res.  solutions:
+ * nrhs*approx_order vec3_soa, index rhs*order + shift; iters_cgm[nrhs],
+ * iters_refine[nrhs*order], true_res[nrhs*order] may be NULL. */
+int ostaple_multishift_batch(const su3_soa *u, const double_soa *phases, double mass, const RationalApprox *approx,
+                             int nrhs, const vec3_soa *sources, vec3_soa *solutions, double res, int max_iter,
+                             double delta_frac, int *iters_cgm, int *iters_refine, double *true_res);
+
 #ifdef __cplusplus
 }
 #endif

@@ -15,7 +15,7 @@ from typing import Sequence
 
 import numpy as np
 
-from .native import FermParam, InverterPackage, RationalApprox, check, inverter_tricks, lib
+from .native import FermParam, InverterPackage, RationalApprox, check, inverter_tricks, lib, set_stout_rho  # noqa: F401
 
 
 def ptr(a) -> int:
@@ -244,3 +244,34 @@ def multiply_backfield_times_force(pars: FermParam, auxmat, pseudo_ipdot) -> Non
 def multiply_conf_times_force_and_take_ta_nophase(u, auxmat, ipdot) -> None:
     lib().multiply_conf_times_force_and_take_ta_nophase(ptr(u), ptr(auxmat), ptr(ipdot))
     check(0, "multiply_conf_times_force_and_take_ta_nophase")
+
+
+# ---- batched solvers ----
+def invert_mixed_batch(u, phases, mass: float, solutions, sources, shifts=None, res: float = 1e-10,
+                       max_iter: int = 100000, delta_frac: float = 0.0) -> dict:
+    """(M^+M + shift_k) x_k = b_k for all k at once (links read once per Dslash per batch of 8)."""
+    nsys = solutions.shape[0]
+    sh = None if shifts is None else np.ascontiguousarray(shifts, dtype=np.float64)
+    it = np.zeros(nsys, np.int32)
+    tr = np.zeros(nsys)
+    nr = np.zeros(nsys, np.int32)
+    st = lib().ostaple_invert_mixed_batch(ptr(u), ptr(phases), mass, nsys, None if sh is None else sh.ctypes.data,
+                                          ptr(solutions), ptr(sources), res, max_iter, delta_frac, it.ctypes.data,
+                                          tr.ctypes.data, nr.ctypes.data)
+    check(0, "ostaple_invert_mixed_batch")
+    return dict(status=st, iters=it, true_res=tr, n_reliable=nr)
+
+
+def multishift_batch(u, phases, mass: float, approx: RationalApprox, sources, solutions, res: float = 1e-10,
+                     max_iter: int = 100000, delta_frac: float = 0.0) -> dict:
+    """All shifts of `approx` for every source: FP32 CG-M then FP64-guaranteed refinement."""
+    nrhs = sources.shape[0]
+    order = approx.approx_order
+    ic = np.zeros(nrhs, np.int32)
+    ir = np.zeros(nrhs * order, np.int32)
+    tr = np.zeros(nrhs * order)
+    st = lib().ostaple_multishift_batch(ptr(u), ptr(phases), mass, C.byref(approx), nrhs, ptr(sources),
+                                        ptr(solutions), res, max_iter, delta_frac, ic.ctypes.data, ir.ctypes.data,
+                                        tr.ctypes.data)
+    check(0, "ostaple_multishift_batch")
+    return dict(status=st, iters_cgm=ic, iters_refine=ir.reshape(nrhs, order), true_res=tr.reshape(nrhs, order))

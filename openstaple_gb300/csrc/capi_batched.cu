@@ -1,0 +1,202 @@
+// capi_batched.cu -- C entry points of the batched solvers.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+#include "batched.cuh"
+#include "dslash.cuh"
+#include "kernels.cuh"
+#include "mixed.cuh"
+#include "runtime.cuh"
+#include "../../include/ostaple_gb300.h"
+
+using namespace ost;
+
+namespace {
+
+typedef double2 Z;
+typedef float2 Zf;
+
+struct Prepared {
+  const float2* u32;
+  const void* ph;
+  int mode;
+};
+
+bool prepare(const Z* u64, const double* ph64, Prepared* out, cudaStream_t st) {
+  const long sh = rt().g.sizeh;
+  float2* u32 = static_cast<float2*>(workspace(WS_LINKS_F32, sizeof(float2) * 48 * size_t(sh)));
+  char* sg = static_cast<char*>(workspace(WS_SIGNS, 256 + 8 * size_t(sh) * sizeof(float)));
+  if (!u32 || !sg) return false;
+  links_to_f32_compact(u64, u32, sh, st);
+  int* flag = reinterpret_cast<int*>(sg);
+  const int one = 1;
+  OST_CUDA(cudaMemcpyAsync(flag, &one, sizeof(int), cudaMemcpyHostToDevice, st));
+  phases_to_signs(ph64, reinterpret_cast<unsigned char*>(sg + 256), flag, sh, st);
+  int exact = 0;
+  OST_CUDA(cudaMemcpyAsync(&exact, flag, sizeof(int), cudaMemcpyDeviceToHost, st));
+  OST_CUDA(cudaStreamSynchronize(st));
+  out->u32 = u32;
+  out->ph = sg + 256;
+  out->mode = PH_SIGN8;
+  if (!exact) {
+    phases_to_f32(ph64, reinterpret_cast<float*>(sg + 256), sh, st);
+    out->mode = PH_ANGLE;
+  }
+  return error_code() == 0;
+}
+
+BatchScal* batch_scalars() {
+  return static_cast<BatchScal*>(workspace(WS_BATCH64, sizeof(BatchScal) + 1024));
+}
+
+// FP32 work vectors of a batch (5 fields per system) and the FP64 work
+// fields (3), all from the workspace.
+bool batch_buffers(int nsys, BatchBuffers* B) {
+  const size_t n = 3 * size_t(rt().g.sizeh);
+  float2* f = static_cast<float2*>(workspace(WS_BATCH, 5 * size_t(BATCH_MAX) * n * sizeof(float2)));
+  double2* d = static_cast<double2*>(workspace(WS_VEC0, 3 * n * sizeof(double2)));
+  if (!f || !d) return false;
+  B->r = f;
+  B->p = f + size_t(BATCH_MAX) * n;
+  B->s = f + 2 * size_t(BATCH_MAX) * n;
+  B->xf = f + 3 * size_t(BATCH_MAX) * n;
+  B->t = f + 4 * size_t(BATCH_MAX) * n;
+  B->r64 = d;
+  B->t64 = d + n;
+  B->t64b = d + 2 * n;
+  B->nsys = nsys;
+  return true;
+}
+
+__global__ void k_f2d_copy(const float2* __restrict__ f, double2* d, long n) {
+  for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n; i += long(gridDim.x) * blockDim.x) {
+    float2 v = f[i];
+    d[i] = make_double2(double(v.x), double(v.y));
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int ostaple_invert_mixed_batch(const su3_soa* u, const double_soa* phases, double mass, int nsys,
+                               const double* shifts, vec3_soa* solutions, const vec3_soa* sources, double res,
+                               int max_iter, double delta_frac, int* iters, double* true_res, int* n_reliable) {
+  if (!require_init("ostaple_invert_mixed_batch")) return INVERTER_FAILURE;
+  if (nsys < 1) { set_error(-11, "ostaple_invert_mixed_batch: nsys %d", nsys); return INVERTER_FAILURE; }
+  cudaStream_t st = rt().stream;
+  const long n = 3L * rt().g.sizeh;
+  const Z* u64 = dev(reinterpret_cast<const Z*>(u), "u");
+  const void* ph = resolve(phases, "phases");
+  Z* x = dev(reinterpret_cast<Z*>(solutions), "solutions");
+  const Z* b = dev(reinterpret_cast<const Z*>(sources), "sources");
+  if (!u64 || !ph || !x || !b) return INVERTER_FAILURE;
+  Prepared pr;
+  if (!prepare(u64, static_cast<const double*>(ph), &pr, st)) return INVERTER_FAILURE;
+  BatchScal* sc = batch_scalars();
+  if (!sc) return INVERTER_FAILURE;
+  int ok = 1;
+  for (int s0 = 0; s0 < nsys; s0 += BATCH_MAX) {
+    const int m = std::min(BATCH_MAX, nsys - s0);
+    BatchBuffers B{};
+    if (!batch_buffers(m, &B)) return INVERTER_FAILURE;
+    B.u64 = u64; B.ph64 = ph; B.u32 = pr.u32; B.ph32 = pr.ph; B.ph32_mode = pr.mode;
+    B.x = x + s0 * n;
+    B.b = b + s0 * n;
+    double m2[BATCH_MAX];
+    for (int k = 0; k < m; ++k) m2[k] = mass * mass + (shifts ? shifts[s0 + k] : 0.0);
+    BatchResult r = batched_mixed_cg(B, m2, res, max_iter, delta_frac > 0 ? delta_frac : 1e-4, sc, st);
+    for (int k = 0; k < m; ++k) {
+      if (iters) iters[s0 + k] = r.iters[k];
+      if (true_res) true_res[s0 + k] = r.true_res[k];
+      if (n_reliable) n_reliable[s0 + k] = r.n_reliable[k];
+      ok &= r.converged[k];
+    }
+  }
+  if (error_code()) return INVERTER_FAILURE;
+  return ok ? INVERTER_SUCCESS : INVERTER_FAILURE;
+}
+
+int ostaple_multishift_batch(const su3_soa* u, const double_soa* phases, double mass, const RationalApprox* approx,
+                             int nrhs, const vec3_soa* sources, vec3_soa* solutions, double res, int max_iter,
+                             double delta_frac, int* iters_cgm, int* iters_refine, double* true_res) {
+  if (!require_init("ostaple_multishift_batch")) return INVERTER_FAILURE;
+  const int order = approx->approx_order;
+  if (nrhs < 1 || nrhs > 4 || order < 1 || order > CGM_MAX_SHIFTS) {
+    set_error(-11, "ostaple_multishift_batch: nrhs %d (1..4), order %d (1..%d)", nrhs, order, CGM_MAX_SHIFTS);
+    return INVERTER_FAILURE;
+  }
+  cudaStream_t st = rt().stream;
+  const long n = 3L * rt().g.sizeh;
+  const Z* u64 = dev(reinterpret_cast<const Z*>(u), "u");
+  const void* ph = resolve(phases, "phases");
+  Z* xs64 = dev(reinterpret_cast<Z*>(solutions), "solutions");
+  const Z* b64 = dev(reinterpret_cast<const Z*>(sources), "sources");
+  if (!u64 || !ph || !xs64 || !b64) return INVERTER_FAILURE;
+  Prepared pr;
+  if (!prepare(u64, static_cast<const double*>(ph), &pr, st)) return INVERTER_FAILURE;
+  // phase A: FP32 CG-M for all right-hand sides together
+  const size_t nv = size_t(nrhs) * (2 * order + 5);
+  float2* f = static_cast<float2*>(workspace(WS_MULTI, nv * n * sizeof(float2)));
+  if (!f) return INVERTER_FAILURE;
+  CgmBatchBuffers C{};
+  C.u32 = pr.u32; C.ph32 = pr.ph; C.ph32_mode = pr.mode; C.nrhs = nrhs; C.nshift = order;
+  float2* bf = f;
+  C.b = bf;
+  C.xs = f + nrhs * n;
+  C.ps = C.xs + size_t(nrhs) * order * n;
+  C.r = C.ps + size_t(nrhs) * order * n;
+  C.p = C.r + nrhs * n;
+  C.s = C.p + nrhs * n;
+  C.t = C.s + nrhs * n;
+  conv_d2f(b64, bf, nrhs * n, st);
+  const double res_a = std::max(res, 1e-5);
+  CgmBatchResult ra = batched_cgm_f32(C, mass * mass, approx->RA_b, res_a, max_iter, st);
+  for (int r = 0; r < nrhs; ++r)
+    if (iters_cgm) iters_cgm[r] = ra.iters[r];
+  // phase B: every (rhs, shift) system refined from the FP32 result to an
+  // FP64 true residual <= res, in batches that group the same shift of all
+  // right-hand sides
+  const long total = long(nrhs) * order;
+  k_f2d_copy<<<8 * rt().num_sms, 256, 0, st>>>(C.xs, xs64, total * n);
+  OST_LAUNCH_CHECK();
+  BatchScal* sc = batch_scalars();
+  if (!sc) return INVERTER_FAILURE;
+  int ok = 1;
+  std::vector<int> sys_rhs, sys_shift;
+  for (int k = 0; k < order; ++k)
+    for (int r = 0; r < nrhs; ++r) { sys_rhs.push_back(r); sys_shift.push_back(k); }
+  // systems of one batch must be contiguous: stage x and b into batch buffers
+  Z* stage = static_cast<Z*>(workspace(WS_MULTI2, 2 * size_t(BATCH_MAX) * n * sizeof(Z)));
+  if (!stage) return INVERTER_FAILURE;
+  Z* sx = stage;
+  Z* sb = stage + size_t(BATCH_MAX) * n;
+  for (size_t s0 = 0; s0 < sys_rhs.size(); s0 += BATCH_MAX) {
+    const int m = int(std::min<size_t>(BATCH_MAX, sys_rhs.size() - s0));
+    double m2[BATCH_MAX];
+    for (int k = 0; k < m; ++k) {
+      const int r = sys_rhs[s0 + k], sh = sys_shift[s0 + k];
+      OST_CUDA(cudaMemcpyAsync(sx + k * n, xs64 + (long(r) * order + sh) * n, n * sizeof(Z), cudaMemcpyDeviceToDevice, st));
+      OST_CUDA(cudaMemcpyAsync(sb + k * n, b64 + r * n, n * sizeof(Z), cudaMemcpyDeviceToDevice, st));
+      m2[k] = mass * mass + approx->RA_b[sh];
+    }
+    BatchBuffers B{};
+    if (!batch_buffers(m, &B)) return INVERTER_FAILURE;
+    B.u64 = u64; B.ph64 = ph; B.u32 = pr.u32; B.ph32 = pr.ph; B.ph32_mode = pr.mode;
+    B.x = sx;
+    B.b = sb;
+    BatchResult rb = batched_mixed_cg(B, m2, res, max_iter, delta_frac > 0 ? delta_frac : 1e-4, sc, st);
+    for (int k = 0; k < m; ++k) {
+      const int r = sys_rhs[s0 + k], sh = sys_shift[s0 + k];
+      OST_CUDA(cudaMemcpyAsync(xs64 + (long(r) * order + sh) * n, sx + k * n, n * sizeof(Z), cudaMemcpyDeviceToDevice, st));
+      if (iters_refine) iters_refine[r * order + sh] = rb.iters[k];
+      if (true_res) true_res[r * order + sh] = rb.true_res[k];
+      ok &= rb.converged[k];
+    }
+  }
+  OST_CUDA(cudaStreamSynchronize(st));
+  if (error_code()) return INVERTER_FAILURE;
+  return ok ? INVERTER_SUCCESS : INVERTER_FAILURE;
+}
+
+}  // extern "C"

@@ -68,6 +68,9 @@ enum WorkspaceSlot {
   WS_FORCE0, WS_FORCE1, WS_FORCE2, WS_FORCE3,
   WS_NET,          // learned preconditioner weights and activations
   WS_NET2,
+  WS_CGM,          // batched multi-shift scalars
+  WS_BATCH,        // batched solver vectors
+  WS_BATCH64,
   WS_NSLOTS
 };
 

@@ -134,6 +134,8 @@ SIGNATURES = {
     "convergence_messages": (None, [_I, _I]),
     "ostaple_invert_mixed": (_I, [_P, _P, _D, _D, _P, _P, _D, _I, _I, _D, C.POINTER(_I), C.POINTER(_D),
                                   C.POINTER(_I)]),
+    "ostaple_invert_mixed_batch": (_I, [_P, _P, _D, _I, _P, _P, _P, _D, _I, _D, _P, _P, _P]),
+    "ostaple_multishift_batch": (_I, [_P, _P, _D, C.POINTER(RationalApprox), _I, _P, _P, _D, _I, _D, _P, _P, _P]),
     "stout_isotropic": (None, [_P, _P, _P, _P, _P, _I]),
     "stout_wrapper": (None, [_P, _P, _I]),
     "exp_minus_QA_times_conf": (None, [_P, _P, _P, _P]),
