@@ -336,6 +336,33 @@ int ostaple_multishift_batch(const su3_soa *u, const double_soa *phases, double 
                              int nrhs, const vec3_soa *sources, vec3_soa *solutions, double res, int max_iter,
                              double delta_frac, int *iters_cgm, int *iters_refine, double *true_res);
 
+/* ---- learned preconditioner (no reference counterpart) -------------------
+ * A linear gauge-covariant network of 4 layers (even -> odd -> even -> odd ->
+ * even), 8 channels per colour: each layer transports its input channels
+ * along the 8 staggered hops (links and staggered signs) and mixes
+ * hops x channels with real weights W[layer][64][8] on the BF16 tensor cores
+ * (FP32 accumulation).  Weights are FP32 masters, 4*64*8 floats, row-major
+ * [layer][hop*8 + in_channel][out_channel].  Phases must be 0 or pi. */
+int ostaple_net_init(unsigned seed, double scale);                 /* uniform in [-scale, scale] */
+int ostaple_net_set_weights(const float *w);
+int ostaple_net_get_weights(float *w);
+/* out = N(in), in/out FP64 vec3_soa on even sites (computed in BF16/FP32) */
+int ostaple_net_apply(const su3_soa *u, const double_soa *phases, const vec3_soa *in, vec3_soa *out);
+/* loss = |N(source) - target|^2 / |target|^2 and dloss/dW into dw[4*64*8] */
+int ostaple_net_gradient(const su3_soa *u, const double_soa *phases, const vec3_soa *source,
+                         const vec3_soa *target, float *dw, double *loss);
+/* full-batch Adam on npairs (source, solution) pairs, one step per epoch;
+ * loss_history[epochs] receives sum_i |N(b_i) - x_i|^2 / (npairs |x_i|^2) */
+int ostaple_net_train(const su3_soa *u, const double_soa *phases, int npairs, const vec3_soa *sources,
+                      const vec3_soa *solutions, int epochs, double lr, double *loss_history);
+/* flexible CG on (M^+M + shift) x = b preconditioned by the network, FP32
+ * iteration with FP64 reliable updates, until the FP64 true residual is
+ * <= res; if it does not converge within max_iter the plain mixed-precision
+ * CG finishes the solve and *used_fallback is set to 1 */
+int ostaple_invert_learned(const su3_soa *u, const double_soa *phases, double mass, double shift,
+                           vec3_soa *solution, const vec3_soa *in, double res, int max_iter, int *iters,
+                           double *true_res, int *used_fallback);
+
 #ifdef __cplusplus
 }
 #endif

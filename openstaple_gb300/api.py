@@ -275,3 +275,50 @@ def multishift_batch(u, phases, mass: float, approx: RationalApprox, sources, so
                                         tr.ctypes.data)
     check(0, "ostaple_multishift_batch")
     return dict(status=st, iters_cgm=ic, iters_refine=ir.reshape(nrhs, order), true_res=tr.reshape(nrhs, order))
+
+
+# ---- learned preconditioner ----
+NET_SHAPE = (4, 64, 8)   # [layer][hop*8 + in_channel][out_channel]
+
+
+def net_init(seed: int = 1, scale: float = 0.05) -> None:
+    check(lib().ostaple_net_init(seed, scale), "ostaple_net_init")
+
+
+def net_set_weights(w: np.ndarray) -> None:
+    w = np.ascontiguousarray(w, dtype=np.float32).reshape(NET_SHAPE)
+    check(lib().ostaple_net_set_weights(w.ctypes.data), "ostaple_net_set_weights")
+
+
+def net_get_weights() -> np.ndarray:
+    w = np.zeros(NET_SHAPE, np.float32)
+    check(lib().ostaple_net_get_weights(w.ctypes.data), "ostaple_net_get_weights")
+    return w
+
+
+def net_apply(u, phases, inp, out) -> None:
+    check(lib().ostaple_net_apply(ptr(u), ptr(phases), ptr(inp), ptr(out)), "ostaple_net_apply")
+
+
+def net_gradient(u, phases, source, target) -> tuple[np.ndarray, float]:
+    dw = np.zeros(NET_SHAPE, np.float32)
+    loss = C.c_double(0)
+    check(lib().ostaple_net_gradient(ptr(u), ptr(phases), ptr(source), ptr(target), dw.ctypes.data, C.byref(loss)),
+          "ostaple_net_gradient")
+    return dw, loss.value
+
+
+def net_train(u, phases, sources, solutions, epochs: int, lr: float) -> np.ndarray:
+    hist = np.zeros(epochs)
+    check(lib().ostaple_net_train(ptr(u), ptr(phases), sources.shape[0], ptr(sources), ptr(solutions), epochs, lr,
+                                  hist.ctypes.data), "ostaple_net_train")
+    return hist
+
+
+def invert_learned(u, phases, mass: float, shift: float, solution, inp, res: float = 1e-10,
+                   max_iter: int = 20000) -> dict:
+    it, tr, fb = C.c_int(0), C.c_double(0), C.c_int(0)
+    st = lib().ostaple_invert_learned(ptr(u), ptr(phases), mass, shift, ptr(solution), ptr(inp), res, max_iter,
+                                      C.byref(it), C.byref(tr), C.byref(fb))
+    check(0, "ostaple_invert_learned")
+    return dict(status=st, iters=it.value, true_res=tr.value, used_fallback=fb.value)

@@ -158,20 +158,26 @@ __global__ void k_b_update(float4* __restrict__ xf, float4* __restrict__ r, cons
     v[k] = 0.f;
   }
   for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n4; i += long(gridDim.x) * blockDim.x) {
+    float4 pv[NS], xv[NS], sv[NS], rv[NS];
+#pragma unroll
+    for (int k = 0; k < NS; ++k) {       // all loads of this element first
+      if (!(mask >> k & 1u)) continue;
+      const long q = k * vs4 + i;
+      pv[k] = p[q]; xv[k] = xf[q];
+      if (!rel[k]) { sv[k] = s[q]; rv[k] = r[q]; }
+    }
 #pragma unroll
     for (int k = 0; k < NS; ++k) {
       if (!(mask >> k & 1u)) continue;
       const long q = k * vs4 + i;
-      float4 pv = p[q], xv = xf[q];
-      xv.x = fmaf(a[k], pv.x, xv.x); xv.y = fmaf(a[k], pv.y, xv.y);
-      xv.z = fmaf(a[k], pv.z, xv.z); xv.w = fmaf(a[k], pv.w, xv.w);
-      xf[q] = xv;
+      xv[k].x = fmaf(a[k], pv[k].x, xv[k].x); xv[k].y = fmaf(a[k], pv[k].y, xv[k].y);
+      xv[k].z = fmaf(a[k], pv[k].z, xv[k].z); xv[k].w = fmaf(a[k], pv[k].w, xv[k].w);
+      xf[q] = xv[k];
       if (!rel[k]) {
-        float4 sv = s[q], rv = r[q];
-        rv.x = fmaf(-a[k], sv.x, rv.x); rv.y = fmaf(-a[k], sv.y, rv.y);
-        rv.z = fmaf(-a[k], sv.z, rv.z); rv.w = fmaf(-a[k], sv.w, rv.w);
-        r[q] = rv;
-        v[k] = fmaf(rv.x, rv.x, fmaf(rv.y, rv.y, fmaf(rv.z, rv.z, fmaf(rv.w, rv.w, v[k]))));
+        rv[k].x = fmaf(-a[k], sv[k].x, rv[k].x); rv[k].y = fmaf(-a[k], sv[k].y, rv[k].y);
+        rv[k].z = fmaf(-a[k], sv[k].z, rv[k].z); rv[k].w = fmaf(-a[k], sv[k].w, rv[k].w);
+        r[q] = rv[k];
+        v[k] = fmaf(rv[k].x, rv[k].x, fmaf(rv[k].y, rv[k].y, fmaf(rv[k].z, rv[k].z, fmaf(rv[k].w, rv[k].w, v[k]))));
       }
     }
   }
@@ -208,13 +214,17 @@ __global__ void k_b_pupdate(float4* __restrict__ p, const float4* __restrict__ r
 #pragma unroll
   for (int k = 0; k < NS; ++k) b[k] = float(sc->beta[k]);
   for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n4; i += long(gridDim.x) * blockDim.x) {
+    float4 pv[NS], rv[NS];
 #pragma unroll
     for (int k = 0; k < NS; ++k) {
       if (!(mask >> k & 1u)) continue;
-      const long q = k * vs4 + i;
-      float4 pv = p[q], rv = r[q];
-      p[q] = make_float4(fmaf(b[k], pv.x, rv.x), fmaf(b[k], pv.y, rv.y), fmaf(b[k], pv.z, rv.z),
-                         fmaf(b[k], pv.w, rv.w));
+      pv[k] = p[k * vs4 + i]; rv[k] = r[k * vs4 + i];
+    }
+#pragma unroll
+    for (int k = 0; k < NS; ++k) {
+      if (!(mask >> k & 1u)) continue;
+      p[k * vs4 + i] = make_float4(fmaf(b[k], pv[k].x, rv[k].x), fmaf(b[k], pv[k].y, rv[k].y),
+                                   fmaf(b[k], pv[k].z, rv[k].z), fmaf(b[k], pv[k].w, rv[k].w));
     }
   }
 }

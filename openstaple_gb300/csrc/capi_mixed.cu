@@ -69,7 +69,7 @@ T* ws_vec(int slot, int k, int nvec) {
 }
 
 MixScal* mix_scalars() {
-  char* p = static_cast<char*>(workspace(WS_SCALARS, 64 * sizeof(double) + 2 * sizeof(MixScal) + 256));
+  char* p = static_cast<char*>(workspace(WS_SCALARS, 64 * sizeof(double) + 4 * sizeof(MixScal) + 256));
   return p ? reinterpret_cast<MixScal*>(p + 64 * sizeof(double)) : nullptr;
 }
 

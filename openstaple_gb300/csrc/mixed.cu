@@ -117,15 +117,29 @@ __global__ void k_mx_update(float4* __restrict__ xf, float4* __restrict__ r, con
   const bool rel = sc->every > 0 ? ((sc->iter + 1) % sc->every == 0) : (delta < sc->frac * lm);
   const float a = float(sc->alpha);
   float v[1] = {0.0f};
-  for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n4; i += long(gridDim.x) * blockDim.x) {
-    float4 pv = p[i], xv = xf[i];
-    xv.x = fmaf(a, pv.x, xv.x); xv.y = fmaf(a, pv.y, xv.y); xv.z = fmaf(a, pv.z, xv.z); xv.w = fmaf(a, pv.w, xv.w);
-    xf[i] = xv;
+  const long stride = long(gridDim.x) * blockDim.x;
+  // two elements per pass, all loads issued before use
+  for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n4; i += 2 * stride) {
+    const long j = i + stride;
+    const bool two = j < n4;
+    float4 pv0 = p[i], xv0 = xf[i], pv1, xv1, sv0, rv0, sv1, rv1;
+    if (two) { pv1 = p[j]; xv1 = xf[j]; }
+    if (!rel) { sv0 = s[i]; rv0 = r[i]; if (two) { sv1 = s[j]; rv1 = r[j]; } }
+    xv0.x = fmaf(a, pv0.x, xv0.x); xv0.y = fmaf(a, pv0.y, xv0.y); xv0.z = fmaf(a, pv0.z, xv0.z); xv0.w = fmaf(a, pv0.w, xv0.w);
+    xf[i] = xv0;
+    if (two) {
+      xv1.x = fmaf(a, pv1.x, xv1.x); xv1.y = fmaf(a, pv1.y, xv1.y); xv1.z = fmaf(a, pv1.z, xv1.z); xv1.w = fmaf(a, pv1.w, xv1.w);
+      xf[j] = xv1;
+    }
     if (!rel) {
-      float4 sv = s[i], rv = r[i];
-      rv.x = fmaf(-a, sv.x, rv.x); rv.y = fmaf(-a, sv.y, rv.y); rv.z = fmaf(-a, sv.z, rv.z); rv.w = fmaf(-a, sv.w, rv.w);
-      r[i] = rv;
-      v[0] = fmaf(rv.x, rv.x, fmaf(rv.y, rv.y, fmaf(rv.z, rv.z, fmaf(rv.w, rv.w, v[0]))));
+      rv0.x = fmaf(-a, sv0.x, rv0.x); rv0.y = fmaf(-a, sv0.y, rv0.y); rv0.z = fmaf(-a, sv0.z, rv0.z); rv0.w = fmaf(-a, sv0.w, rv0.w);
+      r[i] = rv0;
+      v[0] = fmaf(rv0.x, rv0.x, fmaf(rv0.y, rv0.y, fmaf(rv0.z, rv0.z, fmaf(rv0.w, rv0.w, v[0]))));
+      if (two) {
+        rv1.x = fmaf(-a, sv1.x, rv1.x); rv1.y = fmaf(-a, sv1.y, rv1.y); rv1.z = fmaf(-a, sv1.z, rv1.z); rv1.w = fmaf(-a, sv1.w, rv1.w);
+        r[j] = rv1;
+        v[0] = fmaf(rv1.x, rv1.x, fmaf(rv1.y, rv1.y, fmaf(rv1.z, rv1.z, fmaf(rv1.w, rv1.w, v[0]))));
+      }
     }
   }
   double tot[1];
@@ -148,9 +162,13 @@ __global__ void k_mx_pupdate(float4* __restrict__ p, const float4* __restrict__ 
                              int guarded) {
   if (guarded && halted(sc)) return;
   const float b = float(sc->beta);
-  for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n4; i += long(gridDim.x) * blockDim.x) {
-    float4 pv = p[i], rv = r[i];
+  const long stride = long(gridDim.x) * blockDim.x;
+  for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n4; i += 2 * stride) {
+    const long j = i + stride;
+    float4 pv = p[i], rv = r[i], pw, rw;
+    if (j < n4) { pw = p[j]; rw = r[j]; }
     p[i] = make_float4(fmaf(b, pv.x, rv.x), fmaf(b, pv.y, rv.y), fmaf(b, pv.z, rv.z), fmaf(b, pv.w, rv.w));
+    if (j < n4) p[j] = make_float4(fmaf(b, pw.x, rw.x), fmaf(b, pw.y, rw.y), fmaf(b, pw.z, rw.z), fmaf(b, pw.w, rw.w));
   }
 }
 

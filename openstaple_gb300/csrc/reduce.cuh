@@ -21,9 +21,12 @@ struct ReduceWs {
 // Workspace for reductions of up to NV values over at most max_blocks blocks.
 ReduceWs reduce_ws(int nv, int max_blocks);
 
+// Grid for streaming reductions: enough blocks to keep every SM's load
+// queues full (up to 16 blocks of 256 threads per SM), each thread handling a
+// few elements.
 inline int reduce_grid(long n_items) {
-  long b = (n_items + RED_THREADS - 1) / RED_THREADS;
-  long cap = 4L * (rt().num_sms > 0 ? rt().num_sms : 132);
+  long b = (n_items + 2 * RED_THREADS - 1) / (2 * RED_THREADS);
+  long cap = 16L * (rt().num_sms > 0 ? rt().num_sms : 132);
   if (b > cap) b = cap;
   if (b < 1) b = 1;
   return int(b);

@@ -136,6 +136,13 @@ SIGNATURES = {
                                   C.POINTER(_I)]),
     "ostaple_invert_mixed_batch": (_I, [_P, _P, _D, _I, _P, _P, _P, _D, _I, _D, _P, _P, _P]),
     "ostaple_multishift_batch": (_I, [_P, _P, _D, C.POINTER(RationalApprox), _I, _P, _P, _D, _I, _D, _P, _P, _P]),
+    "ostaple_net_init": (_I, [C.c_uint, _D]),
+    "ostaple_net_set_weights": (_I, [_P]),
+    "ostaple_net_get_weights": (_I, [_P]),
+    "ostaple_net_apply": (_I, [_P, _P, _P, _P]),
+    "ostaple_net_gradient": (_I, [_P, _P, _P, _P, _P, C.POINTER(_D)]),
+    "ostaple_net_train": (_I, [_P, _P, _I, _P, _P, _I, _D, _P]),
+    "ostaple_invert_learned": (_I, [_P, _P, _D, _D, _P, _P, _D, _I, C.POINTER(_I), C.POINTER(_D), C.POINTER(_I)]),
     "stout_isotropic": (None, [_P, _P, _P, _P, _P, _I]),
     "stout_wrapper": (None, [_P, _P, _I]),
     "exp_minus_QA_times_conf": (None, [_P, _P, _P, _P]),
