@@ -116,19 +116,55 @@ def test_training_reduces_loss_and_flexible_cg_converges(lat_factory):
     assert np.sqrt(o.norm2(r) / o.norm2(src)) <= 1e-10
 
 
-def test_untrained_network_falls_back_or_converges(lat_factory):
-    """A zero network is a useless preconditioner: the solve must still
-    reach the target, through the plain-CG fallback."""
+def test_zero_network_falls_back_to_plain_cg(lat_factory):
+    """A zero network is no preconditioner at all (its output vanishes): the
+    flexible CG must detect it and the plain CG must finish the solve."""
     dims = (8, 8, 4, 4)
     lat = lat_factory(dims)
     u = F.random_su3_links(dims, 441)
     ph = F.staggered_phases(dims)
     src = F.gaussian_vec3(dims, 442)
     sol = lat.vec3()
-    for a in (u, ph, src, sol):
+    z = lat.vec3()
+    for a in (u, ph, src, sol, z):
         lat.present(a)
+    api.net_init(3, 0.1)
     api.net_set_weights(np.zeros((4, 64, 8), np.float32))
-    res = api.invert_learned(u, ph, 0.1, 0.0, sol, src, 1e-10, 50)
-    assert res["status"] == 1
-    assert res["used_fallback"] == 1
-    assert res["true_res"] <= 1e-10
+    assert np.abs(api.net_get_weights()).max() == 0.0
+    api.net_apply(u, ph, src, z)
+    assert np.abs(lat.update_host(z)).max() == 0.0
+    res = api.invert_learned(u, ph, 0.1, 0.0, sol, src, 1e-10, 200)
+    assert res["used_fallback"] == 1, res
+    assert res["status"] == 1 and res["true_res"] <= 1e-10, res
+
+
+def test_trained_network_gains_over_untrained(lat_factory):
+    """What training buys: flexible-CG iterations with the trained network
+    against the same solver with the untrained (initial) network, and the
+    plain CG iteration count for reference (printed)."""
+    dims = (8, 8, 8, 8)
+    mass = 0.02
+    lat = lat_factory(dims)
+    u = F.random_su3_links(dims, 451)
+    ph = F.staggered_phases(dims)
+    npairs = 8
+    b = np.stack([F.gaussian_vec3(dims, 460 + k) for k in range(npairs)])
+    x = lat.vec3(npairs)
+    src = F.gaussian_vec3(dims, 470)
+    sol = lat.vec3()
+    for a in (u, ph, b, x, src, sol):
+        lat.present(a)
+    info = api.invert_mixed_batch(u, ph, mass, x, b, None, 1e-10)
+    plain_iters = int(info["iters"][0])
+    api.net_init(11, 0.05)
+    before = api.invert_learned(u, ph, mass, 0.0, sol, src, 1e-10, 3000)
+    sol[:] = 0
+    lat.update_device(sol)
+    api.net_init(11, 0.05)
+    api.net_train(u, ph, b, x, 100, 3e-3)
+    after = api.invert_learned(u, ph, mass, 0.0, sol, src, 1e-10, 3000)
+    print(f"plain CG {plain_iters} iterations; flexible CG untrained {before}, trained {after}")
+    assert after["status"] == 1 and after["true_res"] <= 1e-10
+    untrained_cost = before["iters"] if not before["used_fallback"] else 10 ** 9
+    assert after["used_fallback"] == 0
+    assert after["iters"] < untrained_cost
