@@ -348,17 +348,22 @@ int ostaple_net_set_weights(const float *w);
 int ostaple_net_get_weights(float *w);
 /* out = N(in), in/out FP64 vec3_soa on even sites (computed in BF16/FP32) */
 int ostaple_net_apply(const su3_soa *u, const double_soa *phases, const vec3_soa *in, vec3_soa *out);
-/* loss = |N(source) - target|^2 / |target|^2 and dloss/dW into dw[4*64*8] */
-int ostaple_net_gradient(const su3_soa *u, const double_soa *phases, const vec3_soa *source,
-                         const vec3_soa *target, float *dw, double *loss);
-/* full-batch Adam on npairs (source, solution) pairs, one step per epoch;
- * loss_history[epochs] receives sum_i |N(b_i) - x_i|^2 / (npairs |x_i|^2) */
-int ostaple_net_train(const su3_soa *u, const double_soa *phases, int npairs, const vec3_soa *sources,
-                      const vec3_soa *solutions, int epochs, double lr, double *loss_history);
+/* With A = M^+M + shift on even sites (mass, shift as in
+ * ostaple_invert_learned): loss = |A (N(source) - target)|^2 / |source|^2,
+ * the residual that the preconditioned source leaves when target solves
+ * A target = source, and dloss/dW into dw[4*64*8] */
+int ostaple_net_gradient(const su3_soa *u, const double_soa *phases, double mass, double shift,
+                         const vec3_soa *source, const vec3_soa *target, float *dw, double *loss);
+/* full-batch Adam on npairs (source, solution) pairs of A, one step per
+ * epoch; loss_history[epochs] receives the mean of the pairs' losses */
+int ostaple_net_train(const su3_soa *u, const double_soa *phases, double mass, double shift, int npairs,
+                      const vec3_soa *sources, const vec3_soa *solutions, int epochs, double lr,
+                      double *loss_history);
 /* flexible CG on (M^+M + shift) x = b preconditioned by the network, FP32
  * iteration with FP64 reliable updates, until the FP64 true residual is
- * <= res; if it does not converge within max_iter the plain mixed-precision
- * CG finishes the solve and *used_fallback is set to 1 */
+ * <= res; if it does not converge within max_iter, or its residual sets no
+ * new minimum for 500 iterations, the plain mixed-precision CG finishes the
+ * solve and *used_fallback is set to 1 */
 int ostaple_invert_learned(const su3_soa *u, const double_soa *phases, double mass, double shift,
                            vec3_soa *solution, const vec3_soa *in, double res, int max_iter, int *iters,
                            double *true_res, int *used_fallback);

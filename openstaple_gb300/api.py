@@ -300,18 +300,21 @@ def net_apply(u, phases, inp, out) -> None:
     check(lib().ostaple_net_apply(ptr(u), ptr(phases), ptr(inp), ptr(out)), "ostaple_net_apply")
 
 
-def net_gradient(u, phases, source, target) -> tuple[np.ndarray, float]:
+def net_gradient(u, phases, mass: float, source, target, shift: float = 0.0) -> tuple[np.ndarray, float]:
+    """Residual loss |A (N(source) - target)|^2 / |source|^2 of one pair and its
+    weight gradient, A = M^+M + shift."""
     dw = np.zeros(NET_SHAPE, np.float32)
     loss = C.c_double(0)
-    check(lib().ostaple_net_gradient(ptr(u), ptr(phases), ptr(source), ptr(target), dw.ctypes.data, C.byref(loss)),
-          "ostaple_net_gradient")
+    check(lib().ostaple_net_gradient(ptr(u), ptr(phases), mass, shift, ptr(source), ptr(target), dw.ctypes.data,
+                                     C.byref(loss)), "ostaple_net_gradient")
     return dw, loss.value
 
 
-def net_train(u, phases, sources, solutions, epochs: int, lr: float) -> np.ndarray:
+def net_train(u, phases, mass: float, sources, solutions, epochs: int, lr: float, shift: float = 0.0) -> np.ndarray:
+    """Full-batch Adam on (source, solution) pairs of A = M^+M + shift; returns the loss per epoch."""
     hist = np.zeros(epochs)
-    check(lib().ostaple_net_train(ptr(u), ptr(phases), sources.shape[0], ptr(sources), ptr(solutions), epochs, lr,
-                                  hist.ctypes.data), "ostaple_net_train")
+    check(lib().ostaple_net_train(ptr(u), ptr(phases), mass, shift, sources.shape[0], ptr(sources), ptr(solutions),
+                                  epochs, lr, hist.ctypes.data), "ostaple_net_train")
     return hist
 
 

@@ -290,6 +290,7 @@ struct BGraph {
   BatchBuffers key{};
   BatchScal* sc = nullptr;
   int chunk = 0;
+  unsigned long long epoch = 0;
 };
 BGraph g_bgraph;
 cudaStream_t g_bcap = nullptr;
@@ -401,7 +402,7 @@ BatchResult batched_mixed_cg(const BatchBuffers& B, const double* m2, double res
   if (!g_bgraph.exec || g_bgraph.sc != sc || g_bgraph.chunk != chunk || g_bgraph.key.nsys != B.nsys ||
       g_bgraph.key.p != B.p || g_bgraph.key.r != B.r || g_bgraph.key.s != B.s || g_bgraph.key.t != B.t ||
       g_bgraph.key.xf != B.xf || g_bgraph.key.u32 != B.u32 || g_bgraph.key.ph32 != B.ph32 ||
-      g_bgraph.key.ph32_mode != B.ph32_mode) {
+      g_bgraph.key.ph32_mode != B.ph32_mode || g_bgraph.epoch != runtime_epoch()) {
     if (g_bgraph.exec) cudaGraphExecDestroy(g_bgraph.exec);
     cudaGraph_t graph;
     OST_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
@@ -412,6 +413,7 @@ BatchResult batched_mixed_cg(const BatchBuffers& B, const double* m2, double res
     g_bgraph.key = B;
     g_bgraph.sc = sc;
     g_bgraph.chunk = chunk;
+    g_bgraph.epoch = runtime_epoch();
   }
   bool finished[BATCH_MAX] = {false};
   for (int guard = 0; guard < 1000000; ++guard) {

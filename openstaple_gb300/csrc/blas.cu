@@ -18,11 +18,13 @@ static int stream_grid(long n) {
 ReduceWs reduce_ws(int nv, int max_blocks) {
   ReduceWs w;
   size_t bytes = 256 + sizeof(double) * size_t(nv) * size_t(max_blocks);
-  static size_t have = 0;
+  // the ticket counter must read zero before the first reduction into a
+  // freshly allocated buffer; afterwards every reduction leaves it at zero
+  static unsigned long long zeroed_in = 0;
   char* base = static_cast<char*>(workspace(WS_REDUCE, bytes));
-  if (base && bytes > have) {
+  if (base && zeroed_in != runtime_epoch()) {
     cudaMemsetAsync(base, 0, 256, rt().stream);
-    have = bytes;
+    zeroed_in = runtime_epoch();
   }
   w.counter = reinterpret_cast<unsigned int*>(base);
   w.partials = reinterpret_cast<double*>(base + 256);

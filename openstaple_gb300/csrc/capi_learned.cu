@@ -25,6 +25,10 @@ struct NetState {
   float2* z = nullptr;      // network output (FP32 vec3)
   float2* in32 = nullptr;   // network input staging (FP32 vec3)
   float2* x32 = nullptr;    // training target staging
+  float2* e32 = nullptr;    // residual loss: z - x, A (z - x), A A (z - x), operator temporary
+  float2* w32 = nullptr;
+  float2* aw32 = nullptr;
+  float2* t32 = nullptr;
   int adam_t = 0;
 };
 NetState g_net;
@@ -33,7 +37,8 @@ void free_net() {
   NetBuffers& b = g_net.nb;
   for (void* p : {(void*)b.act, (void*)b.grad_a, (void*)b.grad_b, (void*)b.w_master, (void*)b.adam_m,
                   (void*)b.adam_v, (void*)b.dw, (void*)b.dw_partials, (void*)b.w_mma, (void*)b.err, (void*)b.loss,
-                  (void*)g_net.z, (void*)g_net.in32, (void*)g_net.x32})
+                  (void*)g_net.z, (void*)g_net.in32, (void*)g_net.x32, (void*)g_net.e32, (void*)g_net.w32,
+                  (void*)g_net.aw32, (void*)g_net.t32})
     if (p) cudaFree(p);
   g_net = NetState();
 }
@@ -62,7 +67,11 @@ bool ensure_net() {
             cudaMalloc(&b.err, 64) == cudaSuccess && cudaMalloc(&b.loss, 64) == cudaSuccess &&
             cudaMalloc(&g_net.z, 3 * sh * sizeof(float2)) == cudaSuccess &&
             cudaMalloc(&g_net.in32, 3 * sh * sizeof(float2)) == cudaSuccess &&
-            cudaMalloc(&g_net.x32, 3 * sh * sizeof(float2)) == cudaSuccess;
+            cudaMalloc(&g_net.x32, 3 * sh * sizeof(float2)) == cudaSuccess &&
+            cudaMalloc(&g_net.e32, 3 * sh * sizeof(float2)) == cudaSuccess &&
+            cudaMalloc(&g_net.w32, 3 * sh * sizeof(float2)) == cudaSuccess &&
+            cudaMalloc(&g_net.aw32, 3 * sh * sizeof(float2)) == cudaSuccess &&
+            cudaMalloc(&g_net.t32, 3 * sh * sizeof(float2)) == cudaSuccess;
   if (!ok) {
     cudaGetLastError();
     set_error(-5, "learned preconditioner: out of device memory");
@@ -132,20 +141,6 @@ bool check_err(const char* who) {
   return error_code() == 0;
 }
 
-// forward + backward of one (source, target) pair; dW accumulates
-double pair_grad(const Prep& p, const float2* b32, const float2* x32, double xn, int accumulate_loss, cudaStream_t st) {
-  NetBuffers& nb = g_net.nb;
-  apply_net(p, b32, g_net.z, st);
-  net_loss_grad(nb, g_net.z, x32, xn, accumulate_loss, st);
-  float* gout = nb.grad_a;
-  float* gin = nb.grad_b;
-  for (int l = NET_LAYERS - 1; l >= 0; --l) {
-    net_layer_backward(nb, l, p.u32, p.sg, gout, gin, l > 0, st);
-    float* t = gout; gout = gin; gin = t;
-  }
-  return 0.0;
-}
-
 double norm2_f(const float2* v, long n, cudaStream_t st) {
   double* d = static_cast<double*>(workspace(WS_SCALARS, 64 * sizeof(double) + 4 * sizeof(MixScal) + 256));
   blas_norm2<float>(v, n, d + 40, st);
@@ -179,6 +174,29 @@ void mdagm_f64(const Z* u64, const void* ph, Z* out, const Z* in, Z* tmp, double
   launch_dslash<double>(a);
   a.parity = 0; a.epilogue = EPI_MDAGM; a.out = out; a.in = tmp; a.in0 = in; a.mass2 = m2;
   launch_dslash<double>(a);
+}
+
+// Forward + backward of one (source b, solution x) pair; dW accumulates.
+// The loss is the residual of the preconditioned source, |A (N(b) - x)|^2 =
+// |A N(b) - b|^2, scaled by `scale`: it weights the error by A^2, so the
+// network learns A^{-1} where CG needs it (the large eigenvalues, which a
+// few hops can reach) instead of chasing the low modes that dominate x, and
+// the trained map comes out close to Hermitian.
+void pair_grad(const Prep& p, const float2* b32, const float2* x32, double scale, double m2, int accumulate_loss,
+               cudaStream_t st) {
+  NetBuffers& nb = g_net.nb;
+  const long n = 3L * rt().g.sizeh;
+  apply_net(p, b32, g_net.z, st);
+  blas_axpy<float>(x32, -1.0, g_net.z, g_net.e32, n, st);        // e = z - x
+  mdagm_f32(p, g_net.w32, g_net.e32, g_net.t32, m2, st);         // w = A e
+  mdagm_f32(p, g_net.aw32, g_net.w32, g_net.t32, m2, st);        // A w
+  net_residual_loss_grad(nb, g_net.w32, g_net.aw32, scale, accumulate_loss, st);
+  float* gout = nb.grad_a;
+  float* gin = nb.grad_b;
+  for (int l = NET_LAYERS - 1; l >= 0; --l) {
+    net_layer_backward(nb, l, p.u32, p.sg, gout, gin, l > 0, st);
+    float* t = gout; gout = gin; gin = t;
+  }
 }
 
 }  // namespace
@@ -240,8 +258,8 @@ int ostaple_net_apply(const su3_soa* u, const double_soa* phases, const vec3_soa
   return check_err("ostaple_net_apply") ? 0 : -13;
 }
 
-int ostaple_net_gradient(const su3_soa* u, const double_soa* phases, const vec3_soa* source, const vec3_soa* target,
-                         float* dw, double* loss) {
+int ostaple_net_gradient(const su3_soa* u, const double_soa* phases, double mass, double shift,
+                         const vec3_soa* source, const vec3_soa* target, float* dw, double* loss) {
   if (!require_init("ostaple_net_gradient")) return -2;
   if (!ensure_net()) return -5;
   cudaStream_t st = rt().stream;
@@ -253,16 +271,17 @@ int ostaple_net_gradient(const su3_soa* u, const double_soa* phases, const vec3_
   if (!b || !x) return -3;
   conv_d2f(b, g_net.in32, n, st);
   conv_d2f(x, g_net.x32, n, st);
-  const double xn = norm2_f(g_net.x32, n, st);
+  const double bn = norm2_f(g_net.in32, n, st);
   net_zero_dw(g_net.nb, st);
-  pair_grad(p, g_net.in32, g_net.x32, xn, 0, st);
+  pair_grad(p, g_net.in32, g_net.x32, 1.0 / bn, mass * mass + shift, 0, st);
   OST_CUDA(cudaMemcpyAsync(dw, g_net.nb.dw, NET_LAYERS * NET_K * NET_C * sizeof(float), cudaMemcpyDeviceToHost, st));
   OST_CUDA(cudaMemcpyAsync(loss, g_net.nb.loss, sizeof(double), cudaMemcpyDeviceToHost, st));
   return check_err("ostaple_net_gradient") ? 0 : -13;
 }
 
-int ostaple_net_train(const su3_soa* u, const double_soa* phases, int npairs, const vec3_soa* sources,
-                      const vec3_soa* solutions, int epochs, double lr, double* loss_history) {
+int ostaple_net_train(const su3_soa* u, const double_soa* phases, double mass, double shift, int npairs,
+                      const vec3_soa* sources, const vec3_soa* solutions, int epochs, double lr,
+                      double* loss_history) {
   if (!require_init("ostaple_net_train")) return -2;
   if (!ensure_net()) return -5;
   cudaStream_t st = rt().stream;
@@ -272,17 +291,18 @@ int ostaple_net_train(const su3_soa* u, const double_soa* phases, int npairs, co
   const Z* b = dev(reinterpret_cast<const Z*>(sources), "sources");
   const Z* x = dev(reinterpret_cast<const Z*>(solutions), "solutions");
   if (!b || !x || npairs < 1) return -3;
-  std::vector<double> xn(npairs);
+  const double m2 = mass * mass + shift;
+  std::vector<double> bn(npairs);
   for (int i = 0; i < npairs; ++i) {
-    conv_d2f(x + i * n, g_net.x32, n, st);
-    xn[i] = norm2_f(g_net.x32, n, st);
+    conv_d2f(b + i * n, g_net.in32, n, st);
+    bn[i] = norm2_f(g_net.in32, n, st);
   }
   for (int e = 0; e < epochs; ++e) {
     net_zero_dw(g_net.nb, st);
     for (int i = 0; i < npairs; ++i) {
       conv_d2f(b + i * n, g_net.in32, n, st);
       conv_d2f(x + i * n, g_net.x32, n, st);
-      pair_grad(p, g_net.in32, g_net.x32, xn[i] * npairs, i > 0, st);
+      pair_grad(p, g_net.in32, g_net.x32, 1.0 / (bn[i] * npairs), m2, i > 0, st);
     }
     ++g_net.adam_t;
     net_adam_step(g_net.nb, float(lr), 0.9f, 0.999f, 1e-8f, g_net.adam_t, st);
@@ -298,9 +318,10 @@ int ostaple_net_train(const su3_soa* u, const double_soa* phases, int npairs, co
 // Flexible CG (Notay's FCG with one stored direction) on (M^+M + shift) x = b,
 // preconditioned by the network: FP32 iteration, FP64 solution, reliable
 // updates of the residual in FP64, stop when the FP64 true residual is <= res.
-// If the preconditioned iteration does not converge within max_iter (or
-// produces non-finite numbers) the plain mixed-precision CG finishes the solve
-// and *used_fallback is set.
+// If the preconditioned iteration does not converge within max_iter, stalls
+// (no new minimum of the residual for 500 iterations) or produces non-finite
+// numbers, the plain mixed-precision CG finishes the solve and
+// *used_fallback is set.
 int ostaple_invert_learned(const su3_soa* u, const double_soa* phases, double mass, double shift, vec3_soa* solution,
                            const vec3_soa* in, double res, int max_iter, int* iters, double* true_res,
                            int* used_fallback) {
@@ -352,6 +373,12 @@ int ostaple_invert_learned(const su3_soa* u, const double_soa* phases, double ma
   blas_copy<float>(z, pv, n, st);
   mdagm_f32(p, s, pv, t, m2, st);
   double pAp = rdot_f(pv, s, n, st);
+  // stagnation guard: a preconditioner that does not help (an untrained or
+  // zero network) leaves the residual above its best value for long
+  // stretches; hand over to plain CG after STALL iterations without a new best
+  constexpr int STALL = 500;
+  double rr_best = tr2;
+  int it_best = 0;
   while (!converged && it < max_iter) {
     const double pr = rdot_f(pv, r, n, st);
     const double alpha = pr / pAp;
@@ -361,6 +388,8 @@ int ostaple_invert_learned(const su3_soa* u, const double_soa* phases, double ma
     ++it;
     double rr = norm2_f(r, n, st);
     if (!std::isfinite(rr)) { broke = true; break; }
+    if (rr < rr_best) { rr_best = rr; it_best = it; }
+    else if (it - it_best > STALL) break;
     if (rr <= 0.81 * target2 || rr < 1e-4 * rr_ref) {
       tr2 = reliable();
       rr_ref = tr2;

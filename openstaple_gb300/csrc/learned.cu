@@ -348,20 +348,22 @@ __global__ void k_net_input(const float2* __restrict__ r, __nv_bfloat162* __rest
   }
 }
 
-// dL/dz for L = |z - x|^2 / |x|^2 into channel 0 of g (channels 1..7 zeroed);
-// loss accumulated into loss[0]
-__global__ void k_net_loss(const float2* __restrict__ z, const float2* __restrict__ x, float2* __restrict__ gbuf,
-                           long sh, double inv_xn, ReduceWs ws, double* loss, int accumulate) {
+// Residual loss of one pair: with w = A (z - x) and aw = A w (A the
+// Hermitian operator the network preconditions), L = |w|^2 / |b|^2 and
+// dL/dz = 2 A w / |b|^2.  Writes dL/dz into channel 0 of g (channels 1..7
+// zeroed) and accumulates L * scale into loss[0].
+__global__ void k_net_res_loss(const float2* __restrict__ w, const float2* __restrict__ aw, float2* __restrict__ gbuf,
+                               long sh, double scale, ReduceWs ws, double* loss, int accumulate) {
   double v[1] = {0.0};
+  const float g2 = float(2.0 * scale);
   for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < 3 * sh; i += long(gridDim.x) * blockDim.x) {
-    float2 a = z[i], b = x[i];
-    const float dx = a.x - b.x, dy = a.y - b.y;
-    v[0] += double(dx) * dx + double(dy) * dy;
-    gbuf[i] = make_float2(float(2.0 * inv_xn) * dx, float(2.0 * inv_xn) * dy);
+    const float2 a = w[i], b = aw[i];
+    v[0] += double(a.x) * a.x + double(a.y) * a.y;
+    gbuf[i] = make_float2(g2 * b.x, g2 * b.y);
     for (int c = 1; c < NET_C; ++c) gbuf[long(c) * 3 * sh + i] = make_float2(0.f, 0.f);
   }
   double tot[1];
-  if (grid_reduce<1>(v, ws, tot)) loss[0] = (accumulate ? loss[0] : 0.0) + tot[0] * inv_xn;
+  if (grid_reduce<1>(v, ws, tot)) loss[0] = (accumulate ? loss[0] : 0.0) + tot[0] * scale;
 }
 
 __global__ void k_net_adam(float* w, float* m, float* v, const float* dw, int n, float lr, float b1, float b2,
@@ -422,12 +424,12 @@ void net_layer_forward(const NetBuffers& nb, int layer, const float2* u32, const
   OST_LAUNCH_CHECK();
 }
 
-void net_loss_grad(const NetBuffers& nb, const float2* z, const float2* x, double x_norm2, int accumulate,
-                   cudaStream_t st) {
+void net_residual_loss_grad(const NetBuffers& nb, const float2* w, const float2* aw, double scale, int accumulate,
+                            cudaStream_t st) {
   const long sh = rt().g.sizeh;
   const int gr = reduce_grid(3 * sh);
-  k_net_loss<<<gr, RED_THREADS, 0, st>>>(z, x, reinterpret_cast<float2*>(nb.grad_a), sh, 1.0 / x_norm2,
-                                         reduce_ws(1, gr), nb.loss, accumulate);
+  k_net_res_loss<<<gr, RED_THREADS, 0, st>>>(w, aw, reinterpret_cast<float2*>(nb.grad_a), sh, scale,
+                                             reduce_ws(1, gr), nb.loss, accumulate);
   OST_LAUNCH_CHECK();
 }
 

@@ -43,9 +43,10 @@ void net_layer_forward(const NetBuffers& nb, int layer, const float2* u32, const
                        float2* out_f32, cudaStream_t st);
 // input of layer 0 from a float2 vec3 field (channel 0; channels 1..7 zero)
 void net_load_input(const NetBuffers& nb, const float2* r, cudaStream_t st);
-// loss = sum |z - x|^2 / |x|^2 over a batch entry; grad_a (channel 0) = dL/dz
-void net_loss_grad(const NetBuffers& nb, const float2* z, const float2* x, double x_norm2, int accumulate,
-                   cudaStream_t st);
+// residual loss of a batch entry from w = A (z - x) and aw = A w:
+// loss (+)= scale |w|^2, grad_a channel 0 = 2 scale aw, channels 1..7 zero
+void net_residual_loss_grad(const NetBuffers& nb, const float2* w, const float2* aw, double scale, int accumulate,
+                            cudaStream_t st);
 // backward of layer l: grad (output side) -> dW[l] (+=) and grad (input side)
 void net_layer_backward(const NetBuffers& nb, int layer, const float2* u32, const unsigned char* signs,
                         const float* g_out, float* g_in, int need_g_in, cudaStream_t st);

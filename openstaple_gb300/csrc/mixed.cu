@@ -226,6 +226,7 @@ struct GraphCache {
   MixedBuffers key{};
   int chunk = 0;
   MixScal* sc = nullptr;
+  unsigned long long epoch = 0;
 };
 GraphCache g_cache;
 cudaStream_t g_cap = nullptr;
@@ -321,7 +322,8 @@ MixedResult mixed_cg(const MixedBuffers& B, const MixedOptions& o, MixScal* sc, 
     reduce_ws(2, nb > gr ? nb : gr);
   }
   // (re)capture the iteration chunk
-  if (!g_cache.exec || !same_key(g_cache.key, B) || g_cache.chunk != o.chunk || g_cache.sc != sc) {
+  if (!g_cache.exec || !same_key(g_cache.key, B) || g_cache.chunk != o.chunk || g_cache.sc != sc ||
+      g_cache.epoch != runtime_epoch()) {
     if (g_cache.exec) cudaGraphExecDestroy(g_cache.exec);
     g_cache.exec = nullptr;
     cudaGraph_t graph;
@@ -335,6 +337,7 @@ MixedResult mixed_cg(const MixedBuffers& B, const MixedOptions& o, MixScal* sc, 
     g_cache.key = B;
     g_cache.chunk = o.chunk;
     g_cache.sc = sc;
+    g_cache.epoch = runtime_epoch();
   }
 
   const long n4 = n / 2;

@@ -81,12 +81,15 @@ void* resolve(const void* p, const char* what) {
 // ---- workspace ----
 struct Slot { void* p = nullptr; size_t bytes = 0; };
 static Slot g_ws[WS_NSLOTS];
+static unsigned long long g_epoch = 1;
+unsigned long long runtime_epoch() { return g_epoch; }
 
 void* workspace(int slot, size_t bytes) {
   Slot& s = g_ws[slot];
   if (bytes <= s.bytes) return s.p;
   if (s.p) { cudaStreamSynchronize(g_rt.stream); cudaFree(s.p); s.p = nullptr; s.bytes = 0; }
   size_t want = (bytes + 255) & ~size_t(255);
+  ++g_epoch;
   if (cudaMalloc(&s.p, want) != cudaSuccess) {
     cudaGetLastError();
     set_error(-5, "workspace slot %d: cudaMalloc(%zu) failed", slot, want);
@@ -97,6 +100,7 @@ void* workspace(int slot, size_t bytes) {
 }
 
 static void free_workspace() {
+  ++g_epoch;
   for (auto& s : g_ws) { if (s.p) cudaFree(s.p); s.p = nullptr; s.bytes = 0; }
 }
 
@@ -142,6 +146,7 @@ int ostaple_init(int n0, int n1, int n2, int n3) {
   g.fnh0 = FastDiv(uint32_t(g.nh0));
   g.fn1 = FastDiv(uint32_t(n1));
   g.fn2 = FastDiv(uint32_t(n2));
+  ++g_epoch;
   r.initialized = true;
   return 0;
 }

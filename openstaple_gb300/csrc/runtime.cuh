@@ -57,6 +57,11 @@ template <typename T> T* dev(const T* p, const char* what) {
 
 // Growable named device workspace; buffers persist until finalize.
 void* workspace(int slot, size_t bytes);
+// Changes whenever the geometry is set or any workspace buffer is allocated
+// or freed.  State derived from workspace contents or addresses (a zeroed
+// ticket counter, a captured CUDA graph) is valid only for the epoch it was
+// made in: fresh cudaMalloc memory holds whatever was there before.
+unsigned long long runtime_epoch();
 enum WorkspaceSlot {
   WS_REDUCE = 0,   // block partial sums
   WS_SCALARS,      // device-resident solver scalars

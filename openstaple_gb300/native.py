@@ -140,8 +140,8 @@ SIGNATURES = {
     "ostaple_net_set_weights": (_I, [_P]),
     "ostaple_net_get_weights": (_I, [_P]),
     "ostaple_net_apply": (_I, [_P, _P, _P, _P]),
-    "ostaple_net_gradient": (_I, [_P, _P, _P, _P, _P, C.POINTER(_D)]),
-    "ostaple_net_train": (_I, [_P, _P, _I, _P, _P, _I, _D, _P]),
+    "ostaple_net_gradient": (_I, [_P, _P, _D, _D, _P, _P, _P, C.POINTER(_D)]),
+    "ostaple_net_train": (_I, [_P, _P, _D, _D, _I, _P, _P, _I, _D, _P]),
     "ostaple_invert_learned": (_I, [_P, _P, _D, _D, _P, _P, _D, _I, C.POINTER(_I), C.POINTER(_D), C.POINTER(_I)]),
     "stout_isotropic": (None, [_P, _P, _P, _P, _P, _I]),
     "stout_wrapper": (None, [_P, _P, _I]),

@@ -130,13 +130,16 @@ def adjoint_transport(geo: Geometry, U, sg, dh: np.ndarray, p_out: int) -> np.nd
     return g
 
 
-def loss_and_grad(geo: Geometry, U, sg, W, b, x):
-    """FP64 loss |N(b) - x|^2/|x|^2 and dloss/dW of the unrounded network."""
+def loss_and_grad(geo: Geometry, U, sg, W, b, x, apply_a):
+    """FP64 residual loss |A (N(b) - x)|^2 / |b|^2 of the unrounded network and
+    dloss/dW.  apply_a is the Hermitian operator A (M^+M + shift on even
+    sites); dloss/dz = 2 A A (z - x) / |b|^2."""
     z, acts = forward(geo, U, sg, W, b, bf16=False, keep=True)
-    xn = np.sum(np.abs(x) ** 2)
-    loss = np.sum(np.abs(z - x) ** 2) / xn
+    bn = np.sum(np.abs(b) ** 2)
+    w = apply_a(np.ascontiguousarray(z - x))
+    loss = np.sum(np.abs(w) ** 2) / bn
     gz = np.zeros((C, 3, geo.sizeh), np.complex128)
-    gz[0] = 2.0 * (z - x) / xn
+    gz[0] = 2.0 * apply_a(np.ascontiguousarray(w)) / bn
     dW = np.zeros_like(W)
     g = gz
     for layer in range(LAYERS - 1, -1, -1):

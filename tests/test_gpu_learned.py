@@ -4,8 +4,9 @@ the CPU oracle (oracle/learned_ref.py).
 Tolerances: the forward pass is compared with the oracle that rounds
 weights, transported vectors and hidden activations to BF16 at the same
 points (FP32 accumulation order and FP32 links remain): 2e-2 relative in the
-2-norm.  Gradients use BF16 tensor-core operands against the oracle's exact
-FP64 gradient: 5e-2 relative in the 2-norm.  The flexible CG is judged by
+2-norm.  Gradients of the residual loss |A (N(b) - x)|^2 / |b|^2 use BF16
+tensor-core operands and the FP32 operator against the oracle's exact FP64
+gradient: 5e-2 relative in the 2-norm.  The flexible CG is judged by
 the FP64 true residual recomputed by the CPU oracle (<= 1e-10)."""
 import numpy as np
 import pytest
@@ -64,8 +65,11 @@ def test_forward_matches_oracle(lat_factory, dims):
 
 
 def test_gradient_matches_oracle(lat_factory):
+    from oracle import Oracle
     from oracle import learned_ref as R
     dims = (8, 8, 4, 8)
+    mass = 0.1
+    o = Oracle(dims)
     lat = lat_factory(dims)
     u = F.random_su3_links(dims, 411)
     ph = F.staggered_phases(dims)
@@ -75,9 +79,10 @@ def test_gradient_matches_oracle(lat_factory):
         lat.present(a)
     W = _weights(414)
     api.net_set_weights(W)
-    dw, loss = api.net_gradient(u, ph, b, x)
+    dw, loss = api.net_gradient(u, ph, mass, b, x)
     geo = R.Geometry(dims)
-    lo, dwo = R.loss_and_grad(geo, R.full_links(u), R.signs_of(ph), W.astype(np.float64), b, x)
+    A = lambda v: o.mdagm(u, np.ascontiguousarray(v), ph, mass * mass)
+    lo, dwo = R.loss_and_grad(geo, R.full_links(u), R.signs_of(ph), W.astype(np.float64), b, x, A)
     assert abs(loss - lo) <= 3e-2 * lo
     assert nrel(dw, dwo) <= 5e-2
     for layer in range(4):
@@ -102,7 +107,7 @@ def test_training_reduces_loss_and_flexible_cg_converges(lat_factory):
     info = api.invert_mixed_batch(u, ph, mass, x, b, None, 1e-10)
     assert info["status"] == 1
     api.net_init(7, 0.05)
-    hist = api.net_train(u, ph, b, x, 60, 3e-3)
+    hist = api.net_train(u, ph, mass, b, x, 60, 3e-3)
     assert np.all(np.isfinite(hist))
     assert hist[-1] < 0.8 * hist[0]
     src = F.gaussian_vec3(dims, 499)
@@ -138,12 +143,14 @@ def test_zero_network_falls_back_to_plain_cg(lat_factory):
     assert res["status"] == 1 and res["true_res"] <= 1e-10, res
 
 
-def test_trained_network_gains_over_untrained(lat_factory):
-    """What training buys: flexible-CG iterations with the trained network
-    against the same solver with the untrained (initial) network, and the
-    plain CG iteration count for reference (printed)."""
+def test_trained_network_gains_over_plain_cg(lat_factory):
+    """What training buys: the network trained on solver-produced pairs cuts
+    the flexible-CG iteration count well below plain CG's on a new source,
+    without falling back, while the untrained (initial) network does not."""
+    from oracle import Oracle
     dims = (8, 8, 8, 8)
     mass = 0.02
+    o = Oracle(dims)
     lat = lat_factory(dims)
     u = F.random_su3_links(dims, 451)
     ph = F.staggered_phases(dims)
@@ -155,16 +162,21 @@ def test_trained_network_gains_over_untrained(lat_factory):
     for a in (u, ph, b, x, src, sol):
         lat.present(a)
     info = api.invert_mixed_batch(u, ph, mass, x, b, None, 1e-10)
-    plain_iters = int(info["iters"][0])
+    assert info["status"] == 1
+    plain_iters = int(info["iters"].max())
     api.net_init(11, 0.05)
     before = api.invert_learned(u, ph, mass, 0.0, sol, src, 1e-10, 3000)
     sol[:] = 0
     lat.update_device(sol)
     api.net_init(11, 0.05)
-    api.net_train(u, ph, b, x, 100, 3e-3)
+    hist = api.net_train(u, ph, mass, b, x, 200, 3e-3)
     after = api.invert_learned(u, ph, mass, 0.0, sol, src, 1e-10, 3000)
-    print(f"plain CG {plain_iters} iterations; flexible CG untrained {before}, trained {after}")
-    assert after["status"] == 1 and after["true_res"] <= 1e-10
+    lat.update_host(sol)
+    print(f"plain CG {plain_iters} iterations; loss {hist[0]:.4f} -> {hist[-1]:.4f}; "
+          f"flexible CG untrained {before}, trained {after}")
+    assert after["status"] == 1 and after["used_fallback"] == 0, after
+    r = np.ascontiguousarray(src - o.mdagm(u, sol, ph, mass * mass))
+    assert np.sqrt(o.norm2(r) / o.norm2(src)) <= 1e-10
+    assert after["iters"] <= 0.75 * plain_iters
     untrained_cost = before["iters"] if not before["used_fallback"] else 10 ** 9
-    assert after["used_fallback"] == 0
     assert after["iters"] < untrained_cost

@@ -17,11 +17,22 @@ def _setup(dims=(4, 4, 4, 4), seed=5):
     return R, geo, u, ph, U, sg, W
 
 
-def test_gradient_matches_finite_differences():
+def test_gradient_matches_finite_differences(built):
+    """The residual loss |A (N(b) - x)|^2 / |b|^2, A = M^+M from the Dirac oracle."""
+    from oracle import Oracle
     R, geo, u, ph, U, sg, W = _setup()
+    o = Oracle(geo.dims)
+    m2 = 0.1 ** 2
+    A = lambda v: o.mdagm(u, np.ascontiguousarray(v), ph, m2)
     b = F.gaussian_vec3(geo.dims, 1)
     x = F.gaussian_vec3(geo.dims, 2) * 0.1
-    loss, dW = R.loss_and_grad(geo, U, sg, W, b, x)
+    loss, dW = R.loss_and_grad(geo, U, sg, W, b, x, A)
+    bn = np.sum(np.abs(b) ** 2)
+
+    def loss_of(Wv):
+        w = A(R.forward(geo, U, sg, Wv, b, bf16=False) - x)
+        return np.sum(np.abs(w) ** 2) / bn
+    assert abs(loss_of(W) - loss) <= 1e-12 * loss
     rng = np.random.default_rng(0)
     for _ in range(6):
         l, k, n = rng.integers(4), rng.integers(64), rng.integers(8)
@@ -29,10 +40,7 @@ def test_gradient_matches_finite_differences():
         Wp, Wm = W.copy(), W.copy()
         Wp[l, k, n] += e
         Wm[l, k, n] -= e
-        zp = R.forward(geo, U, sg, Wp, b, bf16=False)
-        zm = R.forward(geo, U, sg, Wm, b, bf16=False)
-        xn = np.sum(np.abs(x) ** 2)
-        fd = (np.sum(np.abs(zp - x) ** 2) - np.sum(np.abs(zm - x) ** 2)) / (2 * e * xn)
+        fd = (loss_of(Wp) - loss_of(Wm)) / (2 * e)
         assert abs(fd - dW[l, k, n]) <= 1e-6 * max(1.0, abs(fd))
 
 
