@@ -208,6 +208,16 @@ ostaple_dcomplex scal_prod_global(const vec3_soa *in_vect1, const vec3_soa *in_v
 void scal_prod_global_ri(const vec3_soa *in_vect1, const vec3_soa *in_vect2, double *re_im);
 double real_scal_prod_global(const vec3_soa *in_vect1, const vec3_soa *in_vect2); /* :40 */
 double l2norm2_global(const vec3_soa *in_vect1);                                  /* :42 */
+/* real_scal_prod_global without any device allocation: its scratch (block
+ * partials, ticket counter, result) is a fixed 33,280-byte static device
+ * array, so it can be called where cudaMalloc cannot (while another thread
+ * holds a global-mode stream capture, in loops that must not synchronise the
+ * device, or under a fixed device-memory budget).  Limit: 3*sizeh <= 8,388,608
+ * complex numbers; larger lattices get an error and NAN.  The first call on a
+ * device looks up the array's address and should come before any stream
+ * capture; calls that overlap on the GPU share the array and race.  No
+ * counterpart in the reference. */
+double ostaple_real_scal_prod_global_noalloc(const vec3_soa *in_vect1, const vec3_soa *in_vect2);
 void combine_in1xfactor_plus_in2(const vec3_soa *in_vect1, const double factor,
                                  const vec3_soa *in_vect2, vec3_soa *out);        /* :48 */
 void multiply_fermion_x_doublefactor(vec3_soa *in1, const double factor);         /* :55 */
