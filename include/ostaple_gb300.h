@@ -258,6 +258,17 @@ int multishift_invert(const su3_soa *u, ferm_param *pars, RationalApprox *approx
 void recombine_shifted_vec3_to_vec3(const vec3_soa *in_shifted, const vec3_soa *in, vec3_soa *out,
                                     const RationalApprox *approx);
 
+/* Eigenvalue bounds of M^+M by power iteration (find_min_max.h:14-45):
+ * loc_p / loc_p1 holds a Gaussian start vector on entry; the iteration stops
+ * when the relative change of |p| is <= 1e-5.  find_min_max sets
+ * minmax[0] = m^2 and minmax[1] = the largest eigenvalue. */
+double ker_find_max_eigenvalue_openacc(const su3_soa *u, ferm_param *pars, vec3_soa *loc_r, vec3_soa *loc_h,
+                                       vec3_soa *loc_p);
+double ker_find_min_eigenvalue_openacc(const su3_soa *u, ferm_param *pars, vec3_soa *loc_r, vec3_soa *loc_h,
+                                       vec3_soa *loc_p, double max);
+void find_min_max_eigenvalue_soloopenacc(const su3_soa *u, ferm_param *pars, vec3_soa *loc_r, vec3_soa *loc_h,
+                                         vec3_soa *loc_p1, vec3_soa *loc_p2, double *minmax);
+
 /* Mixed-precision CG: FP32 iteration, FP64 solution and reliable updates of
  * the residual when |r|^2 < inverter_tricks.mixedPrecisionDelta * max|r|^2
  * (inverter_mixedp.c:41-48).  FP32 links come from ip.u_f when set (the

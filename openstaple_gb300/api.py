@@ -164,6 +164,21 @@ def recombine_shifted_vec3_to_vec3(in_shifted, inp, out, approx: RationalApprox)
     check(0, "recombine_shifted_vec3_to_vec3")
 
 
+def find_min_max_eigenvalue_soloopenacc(u, pars: FermParam, loc_r, loc_h, loc_p1, loc_p2) -> np.ndarray:
+    """[m^2, largest eigenvalue of M^+M] by power iteration from the start vector in loc_p1."""
+    mm = np.zeros(2)
+    lib().find_min_max_eigenvalue_soloopenacc(ptr(u), C.byref(pars), ptr(loc_r), ptr(loc_h), ptr(loc_p1),
+                                              ptr(loc_p2), mm.ctypes.data)
+    check(0, "find_min_max_eigenvalue_soloopenacc")
+    return mm
+
+
+def ker_find_min_eigenvalue_openacc(u, pars: FermParam, loc_r, loc_h, loc_p, max_eig: float) -> float:
+    v = lib().ker_find_min_eigenvalue_openacc(ptr(u), C.byref(pars), ptr(loc_r), ptr(loc_h), ptr(loc_p), max_eig)
+    check(0, "ker_find_min_eigenvalue_openacc")
+    return v
+
+
 def set_restarting_every(n: int) -> None:
     inverter_tricks().restartingEvery = int(n)
 

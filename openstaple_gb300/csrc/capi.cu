@@ -407,4 +407,68 @@ void recombine_shifted_vec3_to_vec3(const vec3_soa* in_shifted, const vec3_soa* 
   recombine<double>(xs, vlen(), b, o, rc, vlen(), S());
 }
 
+// ---- eigenvalue bounds of M^+M (the rational approximation's range) ----
+//
+// Power iteration, find_min_max.c:21-92: p <- p/|p|, r = p,
+// p = (m^2 + shift) r - D_eo D_oe r, until the relative change of |p| is at
+// most 1e-5.  p holds the (Gaussian) start vector on entry and the last
+// product on exit, r the last normalised vector; |p| is read back once per
+// iteration for the stopping test, as in the reference.
+static double power_iteration(const char* who, const su3_soa* u, ferm_param* pars, double shift, vec3_soa* loc_r,
+                              vec3_soa* loc_h, vec3_soa* loc_p) {
+  if (!require_init(who)) return NAN;
+  const Z* du = DV(u, "u");
+  Z* p = DVW(loc_p, "loc_p");
+  Z* r = DVW(loc_r, "loc_r");
+  Z* h = DVW(loc_h, "loc_h");
+  const void* ph = resolve(pars->phases, "phases");
+  if (!du || !p || !r || !h || !ph) return NAN;
+  const double m2 = pars->ferm_mass * pars->ferm_mass + shift;
+  double* d = dscal(0);
+  blas_norm2<double>(p, vlen(), d, S());
+  double norm = std::sqrt(readback(d)), rel;
+  int loops = 0;
+  do {
+    blas_scale<double>(p, 1.0 / norm, vlen(), S());
+    blas_copy<double>(p, r, vlen(), S());
+    const double old = norm;
+    mdagm_dev(du, p, r, h, ph, m2);
+    blas_norm2<double>(p, vlen(), d, S());
+    norm = std::sqrt(readback(d));
+    rel = std::fabs(old - norm) / norm;
+    ++loops;
+    if (loops % 100 == 0 && verbosity_lv > 2)
+      printf("        iterations of max computat  = %d, norm = %lf, old_norm = %lf\n", loops, norm, rel);
+    if (loops >= 1000000) {
+      set_error(-15, "%s: power iteration did not settle in %d iterations", who, loops);
+      break;
+    }
+  } while (rel > 1.0e-5 && error_code() == 0);
+  return norm;
+}
+
+double ker_find_max_eigenvalue_openacc(const su3_soa* u, ferm_param* pars, vec3_soa* loc_r, vec3_soa* loc_h,
+                                       vec3_soa* loc_p) {
+  return power_iteration("ker_find_max_eigenvalue_openacc", u, pars, 0.0, loc_r, loc_h, loc_p);
+}
+
+// The reference passes shift = (max - m^2) - m^2 to the shifted matrix and
+// returns max - |p| (find_min_max.c:62-92); kept as it is.  Its caller does
+// not use it: the minimum is set to m^2.
+double ker_find_min_eigenvalue_openacc(const su3_soa* u, ferm_param* pars, vec3_soa* loc_r, vec3_soa* loc_h,
+                                       vec3_soa* loc_p, double max) {
+  const double m2 = pars->ferm_mass * pars->ferm_mass;
+  const double delta = max - m2;
+  return max - power_iteration("ker_find_min_eigenvalue_openacc", u, pars, delta - m2, loc_r, loc_h, loc_p);
+}
+
+void find_min_max_eigenvalue_soloopenacc(const su3_soa* u, ferm_param* pars, vec3_soa* loc_r, vec3_soa* loc_h,
+                                         vec3_soa* loc_p1, vec3_soa* loc_p2, double* minmax) {
+  (void)loc_p2;
+  minmax[0] = pars->ferm_mass * pars->ferm_mass;
+  minmax[1] = ker_find_max_eigenvalue_openacc(u, pars, loc_r, loc_h, loc_p1);
+  if (verbosity_lv > 3)
+    printf("    Computed the min and max eigs : [ min= %.18lf; max= %.18lf ]  \n", minmax[0], minmax[1]);
+}
+
 }  // extern "C"

@@ -130,6 +130,9 @@ SIGNATURES = {
     "multishift_invert": (_I, [_P, C.POINTER(FermParam), C.POINTER(RationalApprox), _P, _P, _D, _P, _P, _P, _P,
                                _P, _I, C.POINTER(_I)]),
     "recombine_shifted_vec3_to_vec3": (None, [_P, _P, _P, C.POINTER(RationalApprox)]),
+    "ker_find_max_eigenvalue_openacc": (_D, [_P, C.POINTER(FermParam), _P, _P, _P]),
+    "ker_find_min_eigenvalue_openacc": (_D, [_P, C.POINTER(FermParam), _P, _P, _P, _D]),
+    "find_min_max_eigenvalue_soloopenacc": (None, [_P, C.POINTER(FermParam), _P, _P, _P, _P, _P]),
     "inverter_mixed_precision": (_I, [InverterPackage, C.POINTER(FermParam), _P, _P, _D, _I, _D, C.POINTER(_I)]),
     "inverter_wrapper": (_I, [InverterPackage, C.POINTER(FermParam), _P, _P, _D, _I, _D, _I]),
     "convergence_messages": (None, [_I, _I]),

@@ -43,6 +43,8 @@ class Oracle:
         "orc_cg": (_I, [_P, _P, _D, _P, _P, _D, _I, _D, _I, C.POINTER(_I)]),
         "orc_cgm": (_I, [_P, _P, _D, _I, _P, _P, _P, _D, _I, C.POINTER(_I)]),
         "orc_recombine": (None, [_P, _P, _P, _I, _D, _P]),
+        "orc_find_max": (_D, [_P, _P, _D, _P, _P, C.POINTER(_I)]),
+        "orc_find_min": (_D, [_P, _P, _D, _P, _P, _D, C.POINTER(_I)]),
         "orc_staples": (None, [_P, _P]),
         "orc_rho_ta": (None, [_P, _P, _P, _D]),
         "orc_exp_times_conf": (None, [_P, _P, _P]),
@@ -112,6 +114,21 @@ class Oracle:
         out = np.zeros((3, self.sizeh), np.complex128)
         self.L.orc_recombine(_p(xs), _p(b), _p(out), len(a), a0, _p(a))
         return out
+
+    def find_max(self, u, ph, mass, p0):
+        """(max, loops, p, r): power iteration from start vector p0."""
+        p = np.ascontiguousarray(p0, dtype=np.complex128).copy()
+        r = np.zeros_like(p)
+        n = C.c_int(0)
+        mx = self.L.orc_find_max(_p(u), _p(ph), mass, _p(p), _p(r), C.byref(n))
+        return mx, n.value, p, r
+
+    def find_min(self, u, ph, mass, p0, max_eig):
+        p = np.ascontiguousarray(p0, dtype=np.complex128).copy()
+        r = np.zeros_like(p)
+        n = C.c_int(0)
+        mn = self.L.orc_find_min(_p(u), _p(ph), mass, _p(p), _p(r), max_eig, C.byref(n))
+        return mn, n.value, p, r
 
     # --- gauge part: su3[8] = complex (8,3,3,sizeh); tamat/thmat = float (8, 8*sizeh) ---
     def su3(self):
@@ -184,6 +201,8 @@ class Reference:
         "ref_cg": (_I, [_P, _P, _D, _P, _P, _D, _I, _D, C.POINTER(_I)]),
         "ref_cgm": (_I, [_P, _P, _D, _I, _D, _P, _P, _P, _P, _D, _I, C.POINTER(_I)]),
         "ref_recombine": (None, [_P, _P, _P, _I, _D, _P]),
+        "ref_find_min_max": (None, [_P, _P, _D, _P, _P, _P]),
+        "ref_find_min": (_D, [_P, _P, _D, _P, _P, _D]),
         "ref_stout_isotropic": (None, [_P, _P, _D]),
         "ref_staples": (None, [_P, _P]),
         "ref_rho_ta": (None, [_P, _P, _P, _D]),
@@ -249,6 +268,20 @@ class Reference:
         out = np.zeros((3, self.sizeh), np.complex128)
         self.L.ref_recombine(_p(xs), _p(b), _p(out), len(a), a0, _p(a))
         return out
+
+    def find_min_max(self, u, ph, mass, p0):
+        """(minmax[2], p, r) from find_min_max_eigenvalue_soloopenacc."""
+        p = np.ascontiguousarray(p0, dtype=np.complex128).copy()
+        r = np.zeros_like(p)
+        mm = np.zeros(2)
+        self.L.ref_find_min_max(_p(u), _p(ph), mass, _p(p), _p(r), _p(mm))
+        return mm, p, r
+
+    def find_min(self, u, ph, mass, p0, max_eig):
+        p = np.ascontiguousarray(p0, dtype=np.complex128).copy()
+        r = np.zeros_like(p)
+        mn = self.L.ref_find_min(_p(u), _p(ph), mass, _p(p), _p(r), max_eig)
+        return mn, p, r
 
     def su3(self):
         return np.zeros((8, 3, 3, self.sizeh), np.complex128)

@@ -243,6 +243,46 @@ int orc_cg(const ocplx *u, const double *ph, double mass, ocplx *x, const ocplx 
   return sqrt(tr) <= res ? 1 : 0;
 }
 
+/* ---- eigenvalue bounds of M^+M: find_min_max.c:21-117 ----
+ * Power iteration: p <- p / |p|, r = p, p = (M^+M + shift) r, until the
+ * relative change of |p| is <= 1e-5.  The largest eigenvalue uses shift 0
+ * (find_min_max.c:21-58).  The smallest one (find_min_max.c:62-92) passes
+ * shift = (max - m^2) - m^2 to the shifted matrix and returns max - |p|,
+ * exactly as the reference does.  p holds the start vector on entry and the
+ * last product on exit; r the last normalised vector. */
+static double power_iteration(const ocplx *u, const double *ph, double m2_plus_shift, ocplx *p, ocplx *r,
+                              int *loops_out)
+{
+  size_t vb = sizeof(ocplx) * 3 * SH;
+  ocplx *h = xmalloc(vb);
+  long i, n = 3 * SH;
+  double norm = sqrt(orc_norm2(p)), rel;
+  int loops = 0;
+  do {
+    double inorm = 1.0 / norm;
+    for (i = 0; i < n; i++) { p[i] = p[i] * inorm; r[i] = p[i]; }
+    double old = norm;
+    orc_mdagm(u, p, r, h, ph, m2_plus_shift);
+    norm = sqrt(orc_norm2(p));
+    rel = fabs(old - norm) / norm;
+    loops++;
+  } while (rel > 1.0e-5);
+  free(h);
+  if (loops_out) *loops_out = loops;
+  return norm;
+}
+
+double orc_find_max(const ocplx *u, const double *ph, double mass, ocplx *p, ocplx *r, int *loops)
+{
+  return power_iteration(u, ph, mass * mass, p, r, loops);
+}
+
+double orc_find_min(const ocplx *u, const double *ph, double mass, ocplx *p, ocplx *r, double max, int *loops)
+{
+  double m2 = mass * mass, delta = max - m2;
+  return max - power_iteration(u, ph, m2 + (delta - m2), p, r, loops);
+}
+
 /* ---- CG-M for (M^+M + b_k) x_k = b: inverter_multishift_full.c:23-252 ----
  * zeta/omega/gamma recurrences of the shifted systems; shift k is frozen
  * once sqrt(delta zeta_k^2 / |b|^2) < 0.95 res; success iff every final

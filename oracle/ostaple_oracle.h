@@ -39,6 +39,8 @@ int orc_cg(const ocplx *u, const double *ph, double mass, ocplx *x, const ocplx 
 int orc_cgm(const ocplx *u, const double *ph, double mass, int order, const double *ra_b, ocplx *xs,
             const ocplx *b, double res, int max_cg, int *cg_out);
 void orc_recombine(const ocplx *xs, const ocplx *b, ocplx *out, int order, double a0, const double *a);
+double orc_find_max(const ocplx *u, const double *ph, double mass, ocplx *p, ocplx *r, int *loops);
+double orc_find_min(const ocplx *u, const double *ph, double mass, ocplx *p, ocplx *r, double max, int *loops);
 
 /* stout smearing and force chain (ostaple_oracle_gauge.c) */
 void orc_gauge_init(int n0, int n1, int n2, int n3);

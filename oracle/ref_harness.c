@@ -31,6 +31,7 @@
 #include "./inverter_full.h"
 #include "./inverter_multishift_full.h"
 #include "./inverter_package.h"
+#include "./find_min_max.h"
 #include "./stouting.h"
 #include "./fermion_force.h"
 #include "./fermion_force_utilities.h"
@@ -154,6 +155,26 @@ int ref_cg(const double *u, double *ph, double mass, double *solution, const dou
                               res, r, h, s, p, max_cg, shift, cg_out);
   free(r); free(h); free(s); free(p);
   return st;
+}
+
+/* ---- eigenvalue bounds (find_min_max.c:21-117) ---- */
+void ref_find_min_max(const double *u, double *ph, double mass, double *p1, double *r, double *minmax)
+{
+  size_t vb = sizeof(vec3_soa);
+  vec3_soa *h = xalloc(vb), *p2 = xalloc(vb);
+  ferm_param fp; make_fp(&fp, ph, mass);
+  find_min_max_eigenvalue_soloopenacc((su3_soa *)u, &fp, (vec3_soa *)r, h, (vec3_soa *)p1, p2, minmax);
+  free(h); free(p2);
+}
+
+double ref_find_min(const double *u, double *ph, double mass, double *p, double *r, double max)
+{
+  size_t vb = sizeof(vec3_soa);
+  vec3_soa *h = xalloc(vb);
+  ferm_param fp; make_fp(&fp, ph, mass);
+  double mn = ker_find_min_eigenvalue_openacc((su3_soa *)u, &fp, (vec3_soa *)r, h, (vec3_soa *)p, max);
+  free(h);
+  return mn;
 }
 
 /* ---- multi-shift CG (inverter_multishift_full.c:23-252) ---- */

@@ -86,9 +86,13 @@ def main(refroot: str) -> None:
         b = np.array(ap["b"]) * mx
         st, n, xs = r.cgm(u, ph, mass, a0, a, b, v, 1e-10, 10000)
         out.update(cgm_status=st, cgm_iters=n, cgm_xs=xs, cgm_recombined=r.recombine(xs, v, a0, a))
+        # eigenvalue bounds (find_min_max.c:21-117) from the source as start vector
+        mm, p, _ = r.find_min_max(u, ph, mass, v)
+        mn, _, _ = r.find_min(u, ph, mass, v, mm[1])
+        out.update(eig_minmax=mm, eig_p=p, eig_min=mn)
         tag = "x".join(map(str, dims))
         np.savez_compressed(HERE / f"dirac_{tag}.npz", **out)
-        print("wrote", tag, "cg", out["cg_iters"], "cgm", out["cgm_iters"])
+        print("wrote", tag, "cg", out["cg_iters"], "cgm", out["cgm_iters"], "eig", mm, mn)
 
 
 if __name__ == "__main__":

@@ -65,6 +65,34 @@ def test_cg_matches_reference(lat_factory, tag):
     assert true_residual(o, u, ph, m, x, b) <= 1e-10
 
 
+@pytest.mark.parametrize("tag", ["4x4x4x4", "4x6x8x10", "8x8x8x8"])
+def test_eigenvalue_bounds_match_reference(lat_factory, tag):
+    """find_min_max_eigenvalue_soloopenacc and ker_find_min_eigenvalue_openacc
+    against the reference's own outputs (golden): the power iteration
+    stops at the same step, so the bound and the last product agree to
+    rounding."""
+    g = load_golden(tag)
+    dims = tuple(int(d) for d in g["dims"])
+    lat = lat_factory(dims)
+    u = F.random_su3_links(dims, int(g["link_seed"]))
+    p1 = F.gaussian_vec3(dims, int(g["src_seed"]))
+    ph = F.staggered_phases(dims)
+    m = float(g["mass"])
+    r, h, p2 = lat.vec3(), lat.vec3(), lat.vec3()
+    for a in (u, ph, p1, r, h, p2):
+        lat.present(a)
+    pars = api.make_ferm_param(m, ph)
+    mm = api.find_min_max_eigenvalue_soloopenacc(u, pars, r, h, p1, p2)
+    lat.update_host(p1)
+    assert mm[0] == m * m
+    assert abs(mm[1] - g["eig_minmax"][1]) <= 1e-12 * mm[1]
+    assert relerr(p1, g["eig_p"]) <= 1e-10
+    p = F.gaussian_vec3(dims, int(g["src_seed"]))
+    lat.present(p)
+    mn = api.ker_find_min_eigenvalue_openacc(u, pars, r, h, p, mm[1])
+    assert abs(mn - float(g["eig_min"])) <= 1e-12 * abs(mn)
+
+
 def test_cg_restarts_and_shift(lat_factory):
     from oracle import Oracle
     dims = (4, 4, 8, 8)

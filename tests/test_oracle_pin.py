@@ -64,6 +64,23 @@ def test_oracle_matches_golden_solvers(built, tag):
     assert relerr(o.recombine(xs, v, a0, a), g["cgm_recombined"]) <= 1e-12
 
 
+@pytest.mark.parametrize("tag", GOLDEN_TAGS)
+def test_oracle_matches_golden_eigenvalue_bounds(built, tag):
+    from oracle import Oracle
+    g = load_golden(tag)
+    dims, u, v = _inputs(g)
+    o = Oracle(dims)
+    ph = o.phases()
+    m = float(g["mass"])
+    mx, loops, p, _ = o.find_max(u, ph, m, v)
+    assert loops > 1
+    assert g["eig_minmax"][0] == m * m
+    assert abs(mx - g["eig_minmax"][1]) <= 1e-13 * mx
+    assert relerr(p, g["eig_p"]) <= 1e-12
+    mn, _, _, _ = o.find_min(u, ph, m, v, mx)
+    assert abs(mn - float(g["eig_min"])) <= 1e-12 * abs(mn)
+
+
 REF_DIMS = [(4, 4, 4, 4), (8, 8, 8, 8), (4, 6, 8, 10)]
 
 
@@ -88,6 +105,11 @@ def test_oracle_matches_compiled_reference(built, dims):
     st2, n2, x2 = r.cg(u, ph, 0.05, v, 1e-10, restart=40)
     assert (st1, n1) == (st2, n2)
     assert relerr(x1, x2) <= 1e-12
+    mm, p2, _ = r.find_min_max(u, ph, 0.05, v)
+    mx, _, p1, _ = o.find_max(u, ph, 0.05, v)
+    assert mm[0] == 0.05 * 0.05
+    assert abs(mx - mm[1]) <= 1e-13 * mx
+    assert relerr(p1, p2) <= 1e-12
 
 
 def test_oracle_cg_max_iterations_failure(built):
