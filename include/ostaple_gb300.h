@@ -209,7 +209,7 @@ void scal_prod_global_ri(const vec3_soa *in_vect1, const vec3_soa *in_vect2, dou
 double real_scal_prod_global(const vec3_soa *in_vect1, const vec3_soa *in_vect2); /* :40 */
 double l2norm2_global(const vec3_soa *in_vect1);                                  /* :42 */
 /* real_scal_prod_global without any device allocation: its scratch (block
- * partials, ticket counter, result) is a fixed 33,280-byte static device
+ * partials, ticket counter, result) is a fixed 33,920-byte static device
  * array, so it can be called where cudaMalloc cannot (while another thread
  * holds a global-mode stream capture, in loops that must not synchronise the
  * device, or under a fixed device-memory budget).  Limit: 3*sizeh <= 8,388,608

@@ -18,92 +18,177 @@ namespace ost {
 
 static constexpr int BT = 128;
 
-// hop term of NS systems at output index idx of parity P, skipping systems
-// whose bit in `mask` is clear.
-template <int NS, int P, int PH>
-OST_D void hop_batch(const Geom& g, const LinkView<float2>& u, const float2* in, long vstride, const void* ph,
-                     int idx, unsigned mask, float2 aux[NS][3]) {
-  typedef unsigned int M;
-  const long sh = g.sizeh;
-  Site s = site_of(g, idx, P);
-  int fwd[4], bwd[4];
-  neighbours(g, s, fwd, bwd);
-#pragma unroll
-  for (int k = 0; k < NS; ++k)
-#pragma unroll
-    for (int c = 0; c < 3; ++c) aux[k][c] = make_float2(0.f, 0.f);
-#pragma unroll
-  for (int half = 0; half < 2; ++half) {
-#pragma unroll
-    for (int mu = 0; mu < 4; ++mu) {
-      const bool back = half == 0;
-      const int dir = back ? 2 * mu + (1 - P) : 2 * mu + P;
-      const int j = back ? bwd[mu] : fwd[mu];      // neighbour holding the input spinor
-      const int li = back ? j : idx;               // index of the link
-      float2 m[6];
-      load_two_rows(u, dir, li, m);
-      M mask_sign;
-      float2 phz = make_float2(1.f, 0.f);
-      bool generic = false;
-      if (PH == PH_SIGN8) {
-        unsigned char sb = __ldg(static_cast<const unsigned char*>(ph) + long(dir) * sh + li);
-        mask_sign = (sb ? 0x80000000u : 0u) ^ (back ? 0x80000000u : 0u);
-      } else {
-        float a = __ldg(static_cast<const float*>(ph) + long(dir) * sh + li);
-        unsigned bits = __float_as_uint(a);
-        if (bits == 0u || bits == PiBits<float>::bits()) {
-          mask_sign = (bits == 0u ? 0u : 0x80000000u) ^ (back ? 0x80000000u : 0u);
-        } else {
-          float sn, cs;
-          sincosf(a, &sn, &cs);
-          phz = make_float2(cs, back ? -sn : sn);
-          mask_sign = back ? 0x80000000u : 0u;
-          generic = true;
-        }
-      }
-#pragma unroll
-      for (int k = 0; k < NS; ++k) {
-        if (!(mask >> k & 1u)) continue;
-        float2 v[3];
-        load_vec(in + k * vstride, sh, j, v);
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-          if (generic) v[c] = cmul(v[c], phz);
-          v[c].x = flip_sign(v[c].x, mask_sign);
-          v[c].y = flip_sign(v[c].y, mask_sign);
-        }
-        if (back) mac_Udag(aux[k], m, v);
-        else mac_U(aux[k], m, v);
-      }
-    }
-  }
+// Layout of the hop kernels.  A thread applies each link it loads to SPL
+// systems (1 for a single system, 2 for up to 4, else 4); the batch is spread over
+// LANES = (NS / SPL rounded up to a power of two) consecutive lanes that
+// share one site and load the same link words in the same instruction, so a
+// link is fetched from memory once per batch.  The link loads, the staggered
+// sign and the rebuilt third row are shared by SPL systems per thread, while
+// the register footprint stays close to a single-system hop's.
+template <int NS>
+struct HopLayout {
+  static constexpr int SPL = NS <= 1 ? 1 : NS <= 4 ? 2 : 4;
+  static constexpr int NL = (NS + SPL - 1) / SPL;
+  static constexpr int LANES = NL <= 1 ? 1 : NL <= 2 ? 2 : NL <= 4 ? 4 : 8;
+  static constexpr int SLOTS = LANES * SPL;   // per-site system slots, >= NS
+};
+
+template <int NS>
+inline int hop_blocks(long sizeh) {
+  return int((sizeh * HopLayout<NS>::LANES + BT - 1) / BT);
+}
+
+OST_D bool batch_active(const BatchScal* sc, int k) {
+  return !(*(volatile const int*)&sc->done[k]) && !(*(volatile const int*)&sc->need_rel[k]);
 }
 
 OST_D unsigned active_mask(const BatchScal* sc) {
   unsigned m = 0;
   for (int k = 0; k < sc->nsys; ++k)
-    if (!(*(volatile const int*)&sc->done[k]) && !(*(volatile const int*)&sc->need_rel[k])) m |= 1u << k;
+    if (batch_active(sc, k)) m |= 1u << k;
   return m;
 }
 
-// t_k = D_oe p_k
+// Hop term at output index idx of parity P for SPL systems whose input
+// fields start at in + sys[j] * vs.  All loads of one hop are issued before
+// its arithmetic; the link, its sign and its rebuilt third row serve all SPL
+// systems.
+template <int SPL, int P, int PH>
+OST_D void hop_multi(const Geom& g, const LinkView<float2>& u, const float2* in, long vs, const int sys[SPL],
+                     const void* phases, int idx, float2 aux[SPL][3]) {
+  const long sh = g.sizeh;
+  Site st = site_of(g, idx, P);
+  int fwd[4], bwd[4];
+  neighbours(g, st, fwd, bwd);
+#pragma unroll
+  for (int j = 0; j < SPL; ++j)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) aux[j][c] = make_float2(0.f, 0.f);
+#pragma unroll
+  for (int hm = 0; hm < 8; ++hm) {
+    const bool back = hm < 4;       // backward hops first, as in the reference
+    const int mu = hm & 3;
+    const int dir = back ? 2 * mu + (1 - P) : 2 * mu + P;
+    const int nb = back ? bwd[mu] : fwd[mu];     // site of the input spinor
+    const int li = back ? nb : idx;              // site the link leaves
+    float2 m[6], v[SPL][3];
+    load_two_rows(u, dir, li, m);
+#pragma unroll
+    for (int j = 0; j < SPL; ++j) load_vec(in + sys[j] * vs, sh, nb, v[j]);
+    unsigned mask = back ? 0x80000000u : 0u;
+    float2 phz = make_float2(1.f, 0.f);
+    bool generic = false;
+    if (PH == PH_SIGN8) {
+      const unsigned char sb = __ldg(static_cast<const unsigned char*>(phases) + long(dir) * sh + li);
+      mask ^= sb ? 0x80000000u : 0u;
+    } else {
+      const float a = __ldcs(static_cast<const float*>(phases) + long(dir) * sh + li);
+      const unsigned bits = __float_as_uint(a);
+      if (bits == PiBits<float>::bits()) {
+        mask ^= 0x80000000u;
+      } else if (bits != 0u) {
+        float sn, cs;
+        sincosf(a, &sn, &cs);
+        phz = make_float2(cs, back ? -sn : sn);
+        generic = true;
+      }
+    }
+    const float2 r20 = conj_cross(m[1], m[5], m[2], m[4]);
+    const float2 r21 = conj_cross(m[2], m[3], m[0], m[5]);
+    const float2 r22 = conj_cross(m[0], m[4], m[1], m[3]);
+#pragma unroll
+    for (int j = 0; j < SPL; ++j) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        if (generic) v[j][c] = cmul(v[j][c], phz);
+        v[j][c].x = flip_sign(v[j][c].x, mask);
+        v[j][c].y = flip_sign(v[j][c].y, mask);
+      }
+      if (back) {
+        cmacc(aux[j][0], m[0], v[j][0]); cmacc(aux[j][0], m[3], v[j][1]); cmacc(aux[j][0], r20, v[j][2]);
+        cmacc(aux[j][1], m[1], v[j][0]); cmacc(aux[j][1], m[4], v[j][1]); cmacc(aux[j][1], r21, v[j][2]);
+        cmacc(aux[j][2], m[2], v[j][0]); cmacc(aux[j][2], m[5], v[j][1]); cmacc(aux[j][2], r22, v[j][2]);
+      } else {
+        cmac(aux[j][0], m[0], v[j][0]); cmac(aux[j][0], m[1], v[j][1]); cmac(aux[j][0], m[2], v[j][2]);
+        cmac(aux[j][1], m[3], v[j][0]); cmac(aux[j][1], m[4], v[j][1]); cmac(aux[j][1], m[5], v[j][2]);
+        cmac(aux[j][2], r20, v[j][0]); cmac(aux[j][2], r21, v[j][1]); cmac(aux[j][2], r22, v[j][2]);
+      }
+    }
+  }
+}
+
+// thread -> (site, lane, first system slot); slots beyond NS read a valid
+// system (slot 0) and discard the result.  Returns idx < sizeh.
+template <int NS>
+OST_D bool hop_thread(long sizeh, int& idx, int& lane, int& ls, int sys[HopLayout<NS>::SPL],
+                      bool valid[HopLayout<NS>::SPL]) {
+  typedef HopLayout<NS> H;
+  const long tid = long(blockIdx.x) * BT + threadIdx.x;
+  idx = int(tid / H::LANES);
+  lane = int(tid % H::LANES);
+  ls = threadIdx.x / H::LANES;
+#pragma unroll
+  for (int j = 0; j < H::SPL; ++j) {
+    const int k = lane * H::SPL + j;
+    valid[j] = k < NS;
+    sys[j] = valid[j] ? k : 0;
+  }
+  return idx < sizeh;
+}
+
+// t_k = D_oe p_k (every system of the batch; converged ones are recomputed
+// harmlessly since t is a temporary)
 template <int NS, int PH>
 __global__ void __launch_bounds__(BT)
 k_b_doe(Geom g, LinkView<float2> u, const void* __restrict__ ph, const float2* __restrict__ p, float2* __restrict__ t,
         long vs, const BatchScal* sc) {
-  const unsigned mask = active_mask(sc);
-  if (!mask) return;
-  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= g.sizeh) return;
-  float2 aux[NS][3];
-  hop_batch<NS, 1, PH>(g, u, p, vs, ph, idx, mask, aux);
+  typedef HopLayout<NS> H;
+  if (!active_mask(sc)) return;
+  int idx, lane, ls, sys[H::SPL];
+  bool valid[H::SPL];
+  const bool live = hop_thread<NS>(g.sizeh, idx, lane, ls, sys, valid);
+  float2 aux[H::SPL][3];
+  if (live) hop_multi<H::SPL, 1, PH>(g, u, p, vs, sys, ph, idx, aux);
+  if (!live) return;
 #pragma unroll
-  for (int k = 0; k < NS; ++k) {
-    if (!(mask >> k & 1u)) continue;
+  for (int j = 0; j < H::SPL; ++j) {
+    if (!valid[j]) continue;
 #pragma unroll
     for (int c = 0; c < 3; ++c)
-      t[k * vs + c * long(g.sizeh) + idx] = make_float2(0.5f * aux[k][c].x, 0.5f * aux[k][c].y);
+      t[sys[j] * vs + c * long(g.sizeh) + idx] = make_float2(0.5f * aux[j][c].x, 0.5f * aux[j][c].y);
   }
+}
+
+// Per-thread values v[j] of system slot lane*SPL + j -> per-system grid totals.
+template <int NS>
+OST_D bool hop_reduce(const float v[HopLayout<NS>::SPL], ReduceWs ws, double tot[HopLayout<NS>::SLOTS]) {
+  typedef HopLayout<NS> H;
+  __shared__ double smem[H::SLOTS * 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nwarps = (blockDim.x + 31) >> 5;
+  float w[H::SPL];
+#pragma unroll
+  for (int j = 0; j < H::SPL; ++j) {
+    w[j] = v[j];
+#pragma unroll
+    for (int o = 16; o >= H::LANES; o >>= 1) w[j] += __shfl_xor_sync(0xffffffffu, w[j], o);
+  }
+  if (lane < H::LANES) {
+#pragma unroll
+    for (int j = 0; j < H::SPL; ++j) smem[(lane * H::SPL + j) * 32 + warp] = double(w[j]);
+  }
+  __syncthreads();
+  double bv[H::SLOTS];
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < H::SLOTS; ++k) {
+      double t = 0.0;
+      for (int q = 0; q < nwarps; ++q) t += smem[k * 32 + q];
+      bv[k] = t;
+    }
+  }
+  __syncthreads();
+  return grid_finish<H::SLOTS>(bv, ws, tot, smem);
 }
 
 // s_k = m2_k p_k - D_eo t_k ; pAp_k ; alpha_k = delta_k / pAp_k
@@ -111,121 +196,129 @@ template <int NS, int PH>
 __global__ void __launch_bounds__(BT)
 k_b_deo_dot(Geom g, LinkView<float2> u, const void* __restrict__ ph, const float2* __restrict__ t,
             const float2* __restrict__ p, float2* __restrict__ s, long vs, BatchScal* sc, ReduceWs ws) {
-  const unsigned mask = active_mask(sc);
-  if (!mask) return;
-  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  float v[NS];
+  typedef HopLayout<NS> H;
+  if (!active_mask(sc)) return;
+  int idx, lane, ls, sys[H::SPL];
+  bool valid[H::SPL];
+  const bool live = hop_thread<NS>(g.sizeh, idx, lane, ls, sys, valid);
+  float v[H::SPL];
+  float2 aux[H::SPL][3];
+  if (live) hop_multi<H::SPL, 0, PH>(g, u, t, vs, sys, ph, idx, aux);
 #pragma unroll
-  for (int k = 0; k < NS; ++k) v[k] = 0.f;
-  if (idx < g.sizeh) {
-    float2 aux[NS][3];
-    hop_batch<NS, 0, PH>(g, u, t, vs, ph, idx, mask, aux);
+  for (int j = 0; j < H::SPL; ++j) {
+    v[j] = 0.f;
+    if (!live || !valid[j]) continue;
+    const float m2 = float(sc->m2[sys[j]]);
 #pragma unroll
-    for (int k = 0; k < NS; ++k) {
-      if (!(mask >> k & 1u)) continue;
-      const float m2 = float(sc->m2[k]);
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        const long q = k * vs + c * long(g.sizeh) + idx;
-        float2 pv = p[q];
-        float2 r = make_float2(fmaf(pv.x, m2, -0.5f * aux[k][c].x), fmaf(pv.y, m2, -0.5f * aux[k][c].y));
-        s[q] = r;
-        v[k] = fmaf(pv.x, r.x, fmaf(pv.y, r.y, v[k]));
-      }
+    for (int c = 0; c < 3; ++c) {
+      const long q = sys[j] * vs + c * long(g.sizeh) + idx;
+      const float2 pv = p[q];
+      const float2 r = make_float2(fmaf(pv.x, m2, -0.5f * aux[j][c].x), fmaf(pv.y, m2, -0.5f * aux[j][c].y));
+      s[q] = r;
+      v[j] = fmaf(pv.x, r.x, fmaf(pv.y, r.y, v[j]));
     }
   }
-  double tot[NS];
-  if (grid_reduce_f32w<NS>(v, ws, tot)) {
+  double tot[H::SLOTS];
+  if (hop_reduce<NS>(v, ws, tot)) {
+    const unsigned mask = active_mask(sc);
     for (int k = 0; k < NS; ++k)
       if (mask >> k & 1u) { sc->pAp[k] = tot[k]; sc->alpha[k] = sc->delta[k] / tot[k]; }
   }
 }
 
-// x_f += alpha p ; unless a reliable update is due: r -= alpha s, lambda = |r|^2
+// Streaming kernels split the grid into one segment of blocks per system.
+inline int seg_blocks(long n4, int nsys) {
+  const int total = reduce_grid(n4 * nsys);
+  const int b = (total + nsys - 1) / nsys;
+  return b < 1 ? 1 : b;
+}
+
+// x_f += alpha p ; unless a reliable update is due: r -= alpha s, lambda = |r|^2,
+// beta = lambda / delta, convergence test (per system)
 template <int NS>
 __global__ void k_b_update(float4* __restrict__ xf, float4* __restrict__ r, const float4* __restrict__ p,
-                           const float4* __restrict__ s, long n4, long vs4, BatchScal* sc, ReduceWs ws) {
-  const unsigned mask = active_mask(sc);
-  if (!mask) return;
-  bool rel[NS];
-  float a[NS], v[NS];
-#pragma unroll
-  for (int k = 0; k < NS; ++k) {
+                           const float4* __restrict__ s, long n4, long vs4, int bps, BatchScal* sc, ReduceWs ws) {
+  const int k = blockIdx.x / bps;
+  const bool act = k < NS && batch_active(sc, k);
+  bool rel = false;
+  float a = 0.f, v = 0.f;
+  if (act) {
     const double delta = sc->delta[k];
     const double lm = sc->last_max[k] > delta ? sc->last_max[k] : delta;
-    rel[k] = sc->every > 0 ? ((sc->iter[k] + 1) % sc->every == 0) : (delta < sc->frac * lm);
-    a[k] = float(sc->alpha[k]);
-    v[k] = 0.f;
-  }
-  for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n4; i += long(gridDim.x) * blockDim.x) {
-    float4 pv[NS], xv[NS], sv[NS], rv[NS];
-#pragma unroll
-    for (int k = 0; k < NS; ++k) {       // all loads of this element first
-      if (!(mask >> k & 1u)) continue;
-      const long q = k * vs4 + i;
-      pv[k] = p[q]; xv[k] = xf[q];
-      if (!rel[k]) { sv[k] = s[q]; rv[k] = r[q]; }
-    }
-#pragma unroll
-    for (int k = 0; k < NS; ++k) {
-      if (!(mask >> k & 1u)) continue;
-      const long q = k * vs4 + i;
-      xv[k].x = fmaf(a[k], pv[k].x, xv[k].x); xv[k].y = fmaf(a[k], pv[k].y, xv[k].y);
-      xv[k].z = fmaf(a[k], pv[k].z, xv[k].z); xv[k].w = fmaf(a[k], pv[k].w, xv[k].w);
-      xf[q] = xv[k];
-      if (!rel[k]) {
-        rv[k].x = fmaf(-a[k], sv[k].x, rv[k].x); rv[k].y = fmaf(-a[k], sv[k].y, rv[k].y);
-        rv[k].z = fmaf(-a[k], sv[k].z, rv[k].z); rv[k].w = fmaf(-a[k], sv[k].w, rv[k].w);
-        r[q] = rv[k];
-        v[k] = fmaf(rv[k].x, rv[k].x, fmaf(rv[k].y, rv[k].y, fmaf(rv[k].z, rv[k].z, fmaf(rv[k].w, rv[k].w, v[k]))));
+    rel = sc->every > 0 ? ((sc->iter[k] + 1) % sc->every == 0) : (delta < sc->frac * lm);
+    a = float(sc->alpha[k]);
+    const long base = k * vs4;
+    const long stride = long(bps) * blockDim.x;
+    for (long i = long(blockIdx.x - k * bps) * blockDim.x + threadIdx.x; i < n4; i += 2 * stride) {
+      const long i2 = i + stride;
+      const bool two = i2 < n4;
+      float4 pv0 = p[base + i], xv0 = xf[base + i], pv1, xv1, sv0, rv0, sv1, rv1;
+      if (two) { pv1 = p[base + i2]; xv1 = xf[base + i2]; }
+      if (!rel) {
+        sv0 = s[base + i]; rv0 = r[base + i];
+        if (two) { sv1 = s[base + i2]; rv1 = r[base + i2]; }
+      }
+      xv0 = make_float4(fmaf(a, pv0.x, xv0.x), fmaf(a, pv0.y, xv0.y), fmaf(a, pv0.z, xv0.z), fmaf(a, pv0.w, xv0.w));
+      xf[base + i] = xv0;
+      if (two) {
+        xv1 = make_float4(fmaf(a, pv1.x, xv1.x), fmaf(a, pv1.y, xv1.y), fmaf(a, pv1.z, xv1.z), fmaf(a, pv1.w, xv1.w));
+        xf[base + i2] = xv1;
+      }
+      if (!rel) {
+        rv0 = make_float4(fmaf(-a, sv0.x, rv0.x), fmaf(-a, sv0.y, rv0.y), fmaf(-a, sv0.z, rv0.z),
+                          fmaf(-a, sv0.w, rv0.w));
+        r[base + i] = rv0;
+        v = fmaf(rv0.x, rv0.x, fmaf(rv0.y, rv0.y, fmaf(rv0.z, rv0.z, fmaf(rv0.w, rv0.w, v))));
+        if (two) {
+          rv1 = make_float4(fmaf(-a, sv1.x, rv1.x), fmaf(-a, sv1.y, rv1.y), fmaf(-a, sv1.z, rv1.z),
+                            fmaf(-a, sv1.w, rv1.w));
+          r[base + i2] = rv1;
+          v = fmaf(rv1.x, rv1.x, fmaf(rv1.y, rv1.y, fmaf(rv1.z, rv1.z, fmaf(rv1.w, rv1.w, v))));
+        }
       }
     }
   }
   double tot[NS];
-  if (grid_reduce_f32w<NS>(v, ws, tot)) {
-    for (int k = 0; k < NS; ++k) {
-      if (!(mask >> k & 1u)) continue;
-      const double delta = sc->delta[k];
-      sc->iter[k] += 1;
-      sc->last_max[k] = sc->last_max[k] > delta ? sc->last_max[k] : delta;
-      if (rel[k]) {
-        sc->need_rel[k] = 1;
+  if (grid_reduce_seg<NS>(v, bps, ws, tot)) {
+    const unsigned mask = active_mask(sc);
+    for (int j = 0; j < NS; ++j) {
+      if (!(mask >> j & 1u)) continue;
+      const double delta = sc->delta[j];
+      const double lm = sc->last_max[j] > delta ? sc->last_max[j] : delta;
+      const bool rj = sc->every > 0 ? ((sc->iter[j] + 1) % sc->every == 0) : (delta < sc->frac * lm);
+      sc->iter[j] += 1;
+      sc->last_max[j] = lm;
+      if (rj) {
+        sc->need_rel[j] = 1;
       } else {
-        sc->lambda[k] = tot[k];
-        sc->beta[k] = tot[k] / delta;
-        sc->delta[k] = tot[k];
-        if (tot[k] <= sc->target2[k] || sc->iter[k] >= sc->max_iter) sc->done[k] = 1;
+        sc->lambda[j] = tot[j];
+        sc->beta[j] = tot[j] / delta;
+        sc->delta[j] = tot[j];
+        if (tot[j] <= sc->target2[j] || sc->iter[j] >= sc->max_iter) sc->done[j] = 1;
       }
     }
   }
 }
 
-// p = r + beta p  (mode 0: active systems; mode 1: system `only`)
+// p = r + beta p for every active system
 template <int NS>
-__global__ void k_b_pupdate(float4* __restrict__ p, const float4* __restrict__ r, long n4, long vs4,
-                            const BatchScal* sc, int only) {
-  unsigned mask;
-  if (only >= 0) mask = 1u << only;
-  else {
-    mask = active_mask(sc);
-    if (!mask) return;
-  }
-  float b[NS];
-#pragma unroll
-  for (int k = 0; k < NS; ++k) b[k] = float(sc->beta[k]);
-  for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n4; i += long(gridDim.x) * blockDim.x) {
-    float4 pv[NS], rv[NS];
-#pragma unroll
-    for (int k = 0; k < NS; ++k) {
-      if (!(mask >> k & 1u)) continue;
-      pv[k] = p[k * vs4 + i]; rv[k] = r[k * vs4 + i];
-    }
-#pragma unroll
-    for (int k = 0; k < NS; ++k) {
-      if (!(mask >> k & 1u)) continue;
-      p[k * vs4 + i] = make_float4(fmaf(b[k], pv[k].x, rv[k].x), fmaf(b[k], pv[k].y, rv[k].y),
-                                   fmaf(b[k], pv[k].z, rv[k].z), fmaf(b[k], pv[k].w, rv[k].w));
-    }
+__global__ void k_b_pupdate(float4* __restrict__ p, const float4* __restrict__ r, long n4, long vs4, int bps,
+                            const BatchScal* sc) {
+  const int k = blockIdx.x / bps;
+  if (k >= NS || !batch_active(sc, k)) return;
+  const float b = float(sc->beta[k]);
+  const long base = k * vs4;
+  const long stride = long(bps) * blockDim.x;
+  for (long i = long(blockIdx.x - k * bps) * blockDim.x + threadIdx.x; i < n4; i += 2 * stride) {
+    const long i2 = i + stride;
+    const bool two = i2 < n4;
+    float4 pv0 = p[base + i], rv0 = r[base + i], pv1, rv1;
+    if (two) { pv1 = p[base + i2]; rv1 = r[base + i2]; }
+    p[base + i] = make_float4(fmaf(b, pv0.x, rv0.x), fmaf(b, pv0.y, rv0.y), fmaf(b, pv0.z, rv0.z),
+                              fmaf(b, pv0.w, rv0.w));
+    if (two)
+      p[base + i2] = make_float4(fmaf(b, pv1.x, rv1.x), fmaf(b, pv1.y, rv1.y), fmaf(b, pv1.z, rv1.z),
+                                 fmaf(b, pv1.w, rv1.w));
   }
 }
 
@@ -309,22 +402,35 @@ template <int NS>
 void enqueue_batch_iteration(const BatchBuffers& B, BatchScal* sc, cudaStream_t st) {
   const Geom& g = rt().g;
   LinkView<float2> u{B.u32, g.sizeh, 6};
-  const int nb = blocks_for(g.sizeh, BT);
+  const int nb = hop_blocks<NS>(g.sizeh);
   const long n = 3L * g.sizeh, n4 = n / 2;
-  const int gr = reduce_grid(n4);
-  ReduceWs ws = reduce_ws(NS, nb > gr ? nb : gr);
+  const int bps = seg_blocks(n4, NS);
+  // one workspace for both reductions: hop (SLOTS x nb partials) and
+  // segments (NS x bps partials)
+  ReduceWs wh = reduce_ws(HopLayout<NS>::SLOTS, nb > NS * bps ? nb : NS * bps);
   if (B.ph32_mode == PH_SIGN8) {
     k_b_doe<NS, PH_SIGN8><<<nb, BT, 0, st>>>(g, u, B.ph32, B.p, B.t, n, sc);
-    k_b_deo_dot<NS, PH_SIGN8><<<nb, BT, 0, st>>>(g, u, B.ph32, B.t, B.p, B.s, n, sc, ws);
+    k_b_deo_dot<NS, PH_SIGN8><<<nb, BT, 0, st>>>(g, u, B.ph32, B.t, B.p, B.s, n, sc, wh);
   } else {
     k_b_doe<NS, PH_ANGLE><<<nb, BT, 0, st>>>(g, u, B.ph32, B.p, B.t, n, sc);
-    k_b_deo_dot<NS, PH_ANGLE><<<nb, BT, 0, st>>>(g, u, B.ph32, B.t, B.p, B.s, n, sc, ws);
+    k_b_deo_dot<NS, PH_ANGLE><<<nb, BT, 0, st>>>(g, u, B.ph32, B.t, B.p, B.s, n, sc, wh);
   }
-  k_b_update<NS><<<gr, RED_THREADS, 0, st>>>(reinterpret_cast<float4*>(B.xf), reinterpret_cast<float4*>(B.r),
-                                              reinterpret_cast<const float4*>(B.p),
-                                              reinterpret_cast<const float4*>(B.s), n4, n4, sc, ws);
-  k_b_pupdate<NS><<<gr, RED_THREADS, 0, st>>>(reinterpret_cast<float4*>(B.p), reinterpret_cast<const float4*>(B.r),
-                                               n4, n4, sc, -1);
+  k_b_update<NS><<<NS * bps, RED_THREADS, 0, st>>>(reinterpret_cast<float4*>(B.xf), reinterpret_cast<float4*>(B.r),
+                                                    reinterpret_cast<const float4*>(B.p),
+                                                    reinterpret_cast<const float4*>(B.s), n4, n4, bps, sc, wh);
+  k_b_pupdate<NS><<<NS * bps, RED_THREADS, 0, st>>>(reinterpret_cast<float4*>(B.p),
+                                                     reinterpret_cast<const float4*>(B.r), n4, n4, bps, sc);
+}
+
+// partial sums that the batched reductions need at most, for pre-sizing the
+// workspace before a graph capture
+inline size_t batch_reduce_partials(long sizeh) {
+  const long n4 = 3L * sizeh / 2;
+  const long hop = long(HopLayout<BATCH_MAX>::SLOTS) * hop_blocks<BATCH_MAX>(sizeh);
+  const long seg = long(BATCH_MAX) * BATCH_MAX * seg_blocks(n4, BATCH_MAX);
+  const long red = long(BATCH_MAX) * reduce_grid(3L * sizeh);
+  long m = hop > seg ? hop : seg;
+  return size_t(m > red ? m : red);
 }
 
 void enqueue_chunk(const BatchBuffers& B, BatchScal* sc, int chunk, cudaStream_t st) {
@@ -367,10 +473,7 @@ BatchResult batched_mixed_cg(const BatchBuffers& B, const double* m2, double res
   OST_CUDA(cudaEventRecord(ev, st));
   OST_CUDA(cudaStreamWaitEvent(g_bcap, ev, 0));
   cudaStream_t cs = g_bcap;
-  {
-    const int nb = blocks_for(g.sizeh, BT), gr = reduce_grid(n);
-    reduce_ws(BATCH_MAX, nb > gr ? nb : gr);
-  }
+  reduce_ws_reserve(batch_reduce_partials(g.sizeh));   // allocated before any capture
   BatchScal init;
   memset(&init, 0, sizeof(init));
   init.frac = delta_frac;
@@ -487,22 +590,26 @@ OST_D unsigned cgm_mask(const CgmScal* sc) {
   return m;
 }
 
+OST_D bool cgm_active(const CgmScal* sc, int r) { return !(*(volatile const int*)&sc->done[r]); }
+
 template <int NR, int PH>
 __global__ void __launch_bounds__(BT)
 k_cgm_doe(Geom g, LinkView<float2> u, const void* __restrict__ ph, const float2* __restrict__ p, float2* __restrict__ t,
           long vs, const CgmScal* sc) {
-  const unsigned mask = cgm_mask(sc);
-  if (!mask) return;
-  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= g.sizeh) return;
-  float2 aux[NR][3];
-  hop_batch<NR, 1, PH>(g, u, p, vs, ph, idx, mask, aux);
+  typedef HopLayout<NR> H;
+  if (!cgm_mask(sc)) return;
+  int idx, lane, ls, sys[H::SPL];
+  bool valid[H::SPL];
+  const bool live = hop_thread<NR>(g.sizeh, idx, lane, ls, sys, valid);
+  float2 aux[H::SPL][3];
+  if (live) hop_multi<H::SPL, 1, PH>(g, u, p, vs, sys, ph, idx, aux);
+  if (!live) return;
 #pragma unroll
-  for (int k = 0; k < NR; ++k) {
-    if (!(mask >> k & 1u)) continue;
+  for (int j = 0; j < H::SPL; ++j) {
+    if (!valid[j]) continue;
 #pragma unroll
     for (int c = 0; c < 3; ++c)
-      t[k * vs + c * long(g.sizeh) + idx] = make_float2(0.5f * aux[k][c].x, 0.5f * aux[k][c].y);
+      t[sys[j] * vs + c * long(g.sizeh) + idx] = make_float2(0.5f * aux[j][c].x, 0.5f * aux[j][c].y);
   }
 }
 
@@ -512,73 +619,72 @@ template <int NR, int PH>
 __global__ void __launch_bounds__(BT)
 k_cgm_deo_dot(Geom g, LinkView<float2> u, const void* __restrict__ ph, const float2* __restrict__ t,
               const float2* __restrict__ p, float2* __restrict__ s, long vs, CgmScal* sc, ReduceWs ws) {
-  const unsigned mask = cgm_mask(sc);
-  if (!mask) return;
-  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  float v[NR];
+  typedef HopLayout<NR> H;
+  if (!cgm_mask(sc)) return;
+  int idx, lane, ls, sys[H::SPL];
+  bool valid[H::SPL];
+  const bool live = hop_thread<NR>(g.sizeh, idx, lane, ls, sys, valid);
+  float v[H::SPL];
+  float2 aux[H::SPL][3];
+  if (live) hop_multi<H::SPL, 0, PH>(g, u, t, vs, sys, ph, idx, aux);
+  const float m2 = float(sc->m2);
 #pragma unroll
-  for (int k = 0; k < NR; ++k) v[k] = 0.f;
-  if (idx < g.sizeh) {
-    const float m2 = float(sc->m2);
-    float2 aux[NR][3];
-    hop_batch<NR, 0, PH>(g, u, t, vs, ph, idx, mask, aux);
+  for (int j = 0; j < H::SPL; ++j) {
+    v[j] = 0.f;
+    if (!live || !valid[j]) continue;
 #pragma unroll
-    for (int k = 0; k < NR; ++k) {
-      if (!(mask >> k & 1u)) continue;
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        const long q = k * vs + c * long(g.sizeh) + idx;
-        float2 pv = p[q];
-        float2 r = make_float2(fmaf(pv.x, m2, -0.5f * aux[k][c].x), fmaf(pv.y, m2, -0.5f * aux[k][c].y));
-        s[q] = r;
-        v[k] = fmaf(pv.x, r.x, fmaf(pv.y, r.y, v[k]));
-      }
+    for (int c = 0; c < 3; ++c) {
+      const long q = sys[j] * vs + c * long(g.sizeh) + idx;
+      const float2 pv = p[q];
+      const float2 r = make_float2(fmaf(pv.x, m2, -0.5f * aux[j][c].x), fmaf(pv.y, m2, -0.5f * aux[j][c].y));
+      s[q] = r;
+      v[j] = fmaf(pv.x, r.x, fmaf(pv.y, r.y, v[j]));
     }
   }
-  double tot[NR];
-  if (grid_reduce_f32w<NR>(v, ws, tot)) {
+  double tot[H::SLOTS];
+  if (hop_reduce<NR>(v, ws, tot)) {
+    const unsigned mask = cgm_mask(sc);
     for (int r = 0; r < sc->nrhs; ++r) {
       if (!(mask >> r & 1u)) continue;
-      for (int k = 0; k < sc->nshift; ++k) sc->flag[r][k] = sc->flag_next[r][k];
+      for (int k2 = 0; k2 < sc->nshift; ++k2) sc->flag[r][k2] = sc->flag_next[r][k2];
       const double alpha = tot[r];
       sc->omega_prev[r] = sc->omega[r];
       const double om = -sc->delta[r] / alpha, omp = sc->omega_prev[r], ga = sc->gamma[r];
       sc->omega[r] = om;
-      for (int k = 0; k < sc->nshift; ++k) {
-        if (!sc->flag[r][k]) continue;
-        const double zi = sc->zi[r][k], zii = sc->zii[r][k];
-        const double z3 = (zi * zii * omp) / (om * ga * (zi - zii) + zi * omp * (1.0 - sc->shift[k] * om));
-        sc->ziii[r][k] = z3;
-        sc->omk[r][k] = om * z3 / zii;
+      for (int k2 = 0; k2 < sc->nshift; ++k2) {
+        if (!sc->flag[r][k2]) continue;
+        const double zi = sc->zi[r][k2], zii = sc->zii[r][k2];
+        const double z3 = (zi * zii * omp) / (om * ga * (zi - zii) + zi * omp * (1.0 - sc->shift[k2] * om));
+        sc->ziii[r][k2] = z3;
+        sc->omk[r][k2] = om * z3 / zii;
       }
     }
   }
 }
 
 // r += omega s ; lambda = |r|^2 ; gamma = lambda/delta ; gamma_k ; freeze
-// decisions for the next iteration (inverter_multishift_full.c:139-171)
+// decisions for the next iteration (inverter_multishift_full.c:139-171).
+// One segment of bps blocks per right-hand side.
 template <int NR>
-__global__ void k_cgm_r(float4* __restrict__ r, const float4* __restrict__ s, long n4, long vs4, CgmScal* sc,
-                        ReduceWs ws) {
-  const unsigned mask = cgm_mask(sc);
-  if (!mask) return;
-  float om[NR], v[NR];
-#pragma unroll
-  for (int k = 0; k < NR; ++k) { om[k] = float(sc->omega[k]); v[k] = 0.f; }
-  for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n4; i += long(gridDim.x) * blockDim.x) {
-#pragma unroll
-    for (int k = 0; k < NR; ++k) {
-      if (!(mask >> k & 1u)) continue;
-      const long q = k * vs4 + i;
-      float4 rv = r[q], sv = s[q];
-      rv.x = fmaf(om[k], sv.x, rv.x); rv.y = fmaf(om[k], sv.y, rv.y);
-      rv.z = fmaf(om[k], sv.z, rv.z); rv.w = fmaf(om[k], sv.w, rv.w);
-      r[q] = rv;
-      v[k] = fmaf(rv.x, rv.x, fmaf(rv.y, rv.y, fmaf(rv.z, rv.z, fmaf(rv.w, rv.w, v[k]))));
+__global__ void k_cgm_r(float4* __restrict__ r, const float4* __restrict__ s, long n4, long vs4, int bps,
+                        CgmScal* sc, ReduceWs ws) {
+  const int rr = blockIdx.x / bps;
+  float v = 0.f;
+  if (rr < NR && cgm_active(sc, rr)) {
+    const float om = float(sc->omega[rr]);
+    const long base = rr * vs4;
+    const long stride = long(bps) * blockDim.x;
+    for (long i = long(blockIdx.x - rr * bps) * blockDim.x + threadIdx.x; i < n4; i += stride) {
+      float4 rv = r[base + i];
+      const float4 sv = s[base + i];
+      rv = make_float4(fmaf(om, sv.x, rv.x), fmaf(om, sv.y, rv.y), fmaf(om, sv.z, rv.z), fmaf(om, sv.w, rv.w));
+      r[base + i] = rv;
+      v = fmaf(rv.x, rv.x, fmaf(rv.y, rv.y, fmaf(rv.z, rv.z, fmaf(rv.w, rv.w, v))));
     }
   }
   double tot[NR];
-  if (grid_reduce_f32w<NR>(v, ws, tot)) {
+  if (grid_reduce_seg<NR>(v, bps, ws, tot)) {
+    const unsigned mask = cgm_mask(sc);
     for (int r2 = 0; r2 < sc->nrhs; ++r2) {
       if (!(mask >> r2 & 1u)) continue;
       const double lambda = tot[r2], delta = sc->delta[r2], om2 = sc->omega[r2];
@@ -602,46 +708,55 @@ __global__ void k_cgm_r(float4* __restrict__ r, const float4* __restrict__ s, lo
   }
 }
 
-// p = r + gamma p ; x_k -= omega_k ps_k ; ps_k = gamma_k ps_k + zeta_k r   (active shifts)
-template <int NR>
-OST_D void cgm_xp_body(float4* __restrict__ p, const float4* __restrict__ r, float4* __restrict__ xs,
-                       float4* __restrict__ ps, long n4, long vs4, const CgmScal* sc, int was_active_mask) {
-  // systems that were active when this iteration started: their flag arrays
-  // hold this iteration's active shifts
-  for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n4; i += long(gridDim.x) * blockDim.x) {
-    for (int rr = 0; rr < sc->nrhs; ++rr) {
-      if (!(was_active_mask >> rr & 1u)) continue;
-      const long q = rr * vs4 + i;
-      const float4 rv = r[q];
-      float4 pv = p[q];
-      const float ga = float(sc->gamma[rr]);
-      p[q] = make_float4(fmaf(ga, pv.x, rv.x), fmaf(ga, pv.y, rv.y), fmaf(ga, pv.z, rv.z), fmaf(ga, pv.w, rv.w));
-      for (int k = 0; k < sc->nshift; ++k) {
-        if (!sc->flag[rr][k]) continue;
-        const long qk = (long(rr) * sc->nshift + k) * vs4 + i;
-        float4 xv = xs[qk], pk = ps[qk];
-        const float om = float(sc->omk[rr][k]), gk = float(sc->gak[rr][k]), z = float(sc->ziii[rr][k]);
-        xv.x = fmaf(-om, pk.x, xv.x); xv.y = fmaf(-om, pk.y, xv.y);
-        xv.z = fmaf(-om, pk.z, xv.z); xv.w = fmaf(-om, pk.w, xv.w);
-        xs[qk] = xv;
-        ps[qk] = make_float4(fmaf(gk, pk.x, z * rv.x), fmaf(gk, pk.y, z * rv.y), fmaf(gk, pk.z, z * rv.z),
-                             fmaf(gk, pk.w, z * rv.w));
-      }
-    }
-  }
-}
-
 // the active-system mask entering an iteration, kept on the device for k_cgm_xp
 __global__ void k_cgm_snapshot(const CgmScal* sc, int* mask_out) {
   if (threadIdx.x == 0 && blockIdx.x == 0) *mask_out = int(cgm_mask(sc));
 }
 
-template <int NR>
+// p = r + gamma p ; x_k -= omega_k ps_k ; ps_k = gamma_k ps_k + zeta_k r over
+// the shifts still active in this iteration.  One segment of bps blocks per
+// right-hand side; a block stages its side's coefficients in shared memory.
+// Only sides that were active when the iteration started are updated.
 __global__ void k_cgm_xp_dev(float4* __restrict__ p, const float4* __restrict__ r, float4* __restrict__ xs,
-                             float4* __restrict__ ps, long n4, long vs4, const CgmScal* sc, const int* mask_in) {
-  const int m = *mask_in;
-  if (!m) return;
-  cgm_xp_body<NR>(p, r, xs, ps, n4, vs4, sc, m);
+                             float4* __restrict__ ps, long n4, long vs4, int bps, const CgmScal* sc,
+                             const int* mask_in) {
+  __shared__ float s_om[CGM_MAX_SHIFTS], s_gk[CGM_MAX_SHIFTS], s_z[CGM_MAX_SHIFTS];
+  __shared__ int s_list[CGM_MAX_SHIFTS], s_n;
+  const int rr = blockIdx.x / bps;
+  if (rr >= sc->nrhs || !(*mask_in >> rr & 1)) return;
+  const int nk = sc->nshift;
+  if (threadIdx.x == 0) {
+    int c = 0;
+    for (int k = 0; k < nk; ++k) {
+      if (!sc->flag[rr][k]) continue;
+      s_list[c] = k;
+      s_om[c] = float(sc->omk[rr][k]);
+      s_gk[c] = float(sc->gak[rr][k]);
+      s_z[c] = float(sc->ziii[rr][k]);
+      ++c;
+    }
+    s_n = c;
+  }
+  __syncthreads();
+  const int na = s_n;
+  const float ga = float(sc->gamma[rr]);
+  const long base = rr * vs4;
+  const long stride = long(bps) * blockDim.x;
+  for (long i = long(blockIdx.x - rr * bps) * blockDim.x + threadIdx.x; i < n4; i += stride) {
+    const float4 rv = r[base + i];
+    const float4 pv = p[base + i];
+    p[base + i] = make_float4(fmaf(ga, pv.x, rv.x), fmaf(ga, pv.y, rv.y), fmaf(ga, pv.z, rv.z), fmaf(ga, pv.w, rv.w));
+    for (int j = 0; j < na; ++j) {
+      const long qk = (long(rr) * nk + s_list[j]) * vs4 + i;
+      float4 xv = xs[qk];
+      const float4 pk = ps[qk];
+      const float om = s_om[j], gk = s_gk[j], z = s_z[j];
+      xv = make_float4(fmaf(-om, pk.x, xv.x), fmaf(-om, pk.y, xv.y), fmaf(-om, pk.z, xv.z), fmaf(-om, pk.w, xv.w));
+      xs[qk] = xv;
+      ps[qk] = make_float4(fmaf(gk, pk.x, z * rv.x), fmaf(gk, pk.y, z * rv.y), fmaf(gk, pk.z, z * rv.z),
+                           fmaf(gk, pk.w, z * rv.w));
+    }
+  }
 }
 
 namespace {
@@ -650,10 +765,10 @@ template <int NR>
 void enqueue_cgm_iteration(const CgmBatchBuffers& B, CgmScal* sc, int* snap, cudaStream_t st) {
   const Geom& g = rt().g;
   LinkView<float2> u{B.u32, g.sizeh, 6};
-  const int nb = blocks_for(g.sizeh, BT);
+  const int nb = hop_blocks<NR>(g.sizeh);
   const long n = 3L * g.sizeh, n4 = n / 2;
-  const int gr = reduce_grid(n4);
-  ReduceWs ws = reduce_ws(NR, nb > gr ? nb : gr);
+  const int bps = seg_blocks(n4, NR);
+  ReduceWs ws = reduce_ws(HopLayout<NR>::SLOTS, nb > NR * bps ? nb : NR * bps);
   k_cgm_snapshot<<<1, 32, 0, st>>>(sc, snap);
   if (B.ph32_mode == PH_SIGN8) {
     k_cgm_doe<NR, PH_SIGN8><<<nb, BT, 0, st>>>(g, u, B.ph32, B.p, B.t, n, sc);
@@ -662,11 +777,13 @@ void enqueue_cgm_iteration(const CgmBatchBuffers& B, CgmScal* sc, int* snap, cud
     k_cgm_doe<NR, PH_ANGLE><<<nb, BT, 0, st>>>(g, u, B.ph32, B.p, B.t, n, sc);
     k_cgm_deo_dot<NR, PH_ANGLE><<<nb, BT, 0, st>>>(g, u, B.ph32, B.t, B.p, B.s, n, sc, ws);
   }
-  k_cgm_r<NR><<<gr, RED_THREADS, 0, st>>>(reinterpret_cast<float4*>(B.r), reinterpret_cast<const float4*>(B.s), n4,
-                                          n4, sc, ws);
-  k_cgm_xp_dev<NR><<<gr, RED_THREADS, 0, st>>>(reinterpret_cast<float4*>(B.p), reinterpret_cast<const float4*>(B.r),
-                                               reinterpret_cast<float4*>(B.xs), reinterpret_cast<float4*>(B.ps), n4,
-                                               n4, sc, snap);
+  k_cgm_r<NR><<<NR * bps, RED_THREADS, 0, st>>>(reinterpret_cast<float4*>(B.r), reinterpret_cast<const float4*>(B.s),
+                                                n4, n4, bps, sc, ws);
+  // the x/p update streams nshift+1 fields per side: give it more blocks
+  const int bxp = seg_blocks(n4 * (B.nshift + 1), NR);
+  k_cgm_xp_dev<<<NR * bxp, RED_THREADS, 0, st>>>(reinterpret_cast<float4*>(B.p), reinterpret_cast<const float4*>(B.r),
+                                                 reinterpret_cast<float4*>(B.xs), reinterpret_cast<float4*>(B.ps), n4,
+                                                 n4, bxp, sc, snap);
 }
 
 }  // namespace
@@ -687,10 +804,7 @@ CgmBatchResult batched_cgm_f32(const CgmBatchBuffers& B, double mass2, const dou
   CgmScal* sc = reinterpret_cast<CgmScal*>(ws);
   int* snap = reinterpret_cast<int*>(ws + sizeof(CgmScal) + 64);
   double* norms = reinterpret_cast<double*>(ws + sizeof(CgmScal) + 128);
-  {
-    const int nb = blocks_for(g.sizeh, BT), gr = reduce_grid(n);
-    reduce_ws(BATCH_MAX, nb > gr ? nb : gr);
-  }
+  reduce_ws_reserve(batch_reduce_partials(g.sizeh));   // allocated before any capture
   CgmScal* h = nullptr;
   OST_CUDA(cudaMallocHost(&h, sizeof(CgmScal)));
   memset(h, 0, sizeof(CgmScal));

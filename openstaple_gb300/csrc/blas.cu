@@ -16,20 +16,35 @@ static int stream_grid(long n) {
 }
 
 ReduceWs reduce_ws(int nv, int max_blocks) {
+  // layout: RED_COUNTERS ticket counters | nv*max_blocks partials | nv*max_groups group totals
   ReduceWs w;
-  size_t bytes = 256 + sizeof(double) * size_t(nv) * size_t(max_blocks);
-  // the ticket counter must read zero before the first reduction into a
-  // freshly allocated buffer; afterwards every reduction leaves it at zero
+  if (max_blocks > RED_GROUP * (RED_COUNTERS - 1)) {
+    set_error(-16, "reduction over %d blocks exceeds the workspace's %d", max_blocks, RED_GROUP * (RED_COUNTERS - 1));
+    max_blocks = RED_GROUP * (RED_COUNTERS - 1);
+  }
+  const int max_groups = (max_blocks + RED_GROUP - 1) / RED_GROUP;
+  const size_t head = sizeof(unsigned int) * RED_COUNTERS;
+  size_t bytes = head + sizeof(double) * size_t(nv) * (size_t(max_blocks) + size_t(max_groups));
+  // the ticket counters must read zero before the first reduction into a
+  // freshly allocated buffer; afterwards every reduction leaves them at zero
   static unsigned long long zeroed_in = 0;
   char* base = static_cast<char*>(workspace(WS_REDUCE, bytes));
   if (base && zeroed_in != runtime_epoch()) {
-    cudaMemsetAsync(base, 0, 256, rt().stream);
+    cudaMemsetAsync(base, 0, head, rt().stream);
     zeroed_in = runtime_epoch();
   }
   w.counter = reinterpret_cast<unsigned int*>(base);
-  w.partials = reinterpret_cast<double*>(base + 256);
+  w.partials = reinterpret_cast<double*>(base + head);
+  w.gpartials = w.partials + size_t(nv) * max_blocks;
   w.max_blocks = max_blocks;
+  w.max_groups = max_groups;
   return w;
+}
+
+void reduce_ws_reserve(size_t partials) {
+  // nv*max_blocks <= partials implies nv*(max_blocks + max_groups) <= partials*(1 + 1/64) + 8*nv
+  const size_t bytes = sizeof(unsigned int) * RED_COUNTERS + sizeof(double) * (partials + partials / RED_GROUP + 64);
+  workspace(WS_REDUCE, bytes);
 }
 
 // ---- reductions ----

@@ -18,16 +18,21 @@
 
 namespace ost {
 
-// 4096 block partials + 64 header doubles (counter at word 0, result at
-// word 8): 33,280 bytes per device.
+// Layout in doubles: [0, 64) ticket counters (the final one and one per
+// group of blocks, 65 used), [64] the result, [80, 80 + 4096) block
+// partials, then 64 group totals: 33,920 bytes per device.
 static constexpr int NOALLOC_MAX_BLOCKS = 4096;
-static constexpr int NOALLOC_HEADER = 64;
+static constexpr int NOALLOC_MAX_GROUPS = NOALLOC_MAX_BLOCKS / RED_GROUP;
+static constexpr int NOALLOC_RESULT = 64;
+static constexpr int NOALLOC_HEADER = 80;
+static_assert((NOALLOC_MAX_GROUPS + 1) * sizeof(unsigned int) <= NOALLOC_RESULT * sizeof(double),
+              "ticket counters overlap the result slot");
 static constexpr int NOALLOC_THREADS = 256;
 static constexpr int NOALLOC_PER_THREAD = 8;                                     // complex numbers per thread
 static constexpr long NOALLOC_PER_BLOCK = long(NOALLOC_THREADS) * NOALLOC_PER_THREAD;
 static constexpr long NOALLOC_MAX_N = NOALLOC_MAX_BLOCKS * NOALLOC_PER_BLOCK;     // 8,388,608 complex numbers
 
-static __device__ __align__(256) double g_noalloc_scratch[NOALLOC_HEADER + NOALLOC_MAX_BLOCKS];
+static __device__ __align__(256) double g_noalloc_scratch[NOALLOC_HEADER + NOALLOC_MAX_BLOCKS + NOALLOC_MAX_GROUPS];
 
 // Each block reduces a fixed chunk of NOALLOC_PER_BLOCK complex numbers, so
 // the number of partials is n / chunk and the scratch bounds n.
@@ -46,9 +51,11 @@ __global__ void k_rdot_noalloc(const double2* __restrict__ a, const double2* __r
   ReduceWs ws;
   ws.counter = reinterpret_cast<unsigned int*>(scratch);
   ws.partials = scratch + NOALLOC_HEADER;
+  ws.gpartials = ws.partials + NOALLOC_MAX_BLOCKS;
   ws.max_blocks = NOALLOC_MAX_BLOCKS;
+  ws.max_groups = NOALLOC_MAX_GROUPS;
   double tot[1];
-  if (grid_reduce<1>(v, ws, tot)) scratch[8] = tot[0];
+  if (grid_reduce<1>(v, ws, tot)) scratch[NOALLOC_RESULT] = tot[0];
 }
 
 }  // namespace ost
@@ -90,13 +97,13 @@ extern "C" double ostaple_real_scal_prod_global_noalloc(const vec3_soa* in_vect1
   const double2* b = dev(reinterpret_cast<const double2*>(in_vect2), "in_vect2");
   if (!a || !b) return NAN;
   cudaStream_t st = rt().stream;
-  // the array keeps the previous call's contents: the ticket counter must start at zero
-  OST_CUDA(cudaMemsetAsync(scratch, 0, sizeof(unsigned int), st));
+  // the array keeps the previous call's contents: the ticket counters must start at zero
+  OST_CUDA(cudaMemsetAsync(scratch, 0, NOALLOC_RESULT * sizeof(double), st));
   const int grid = int((n + NOALLOC_PER_BLOCK - 1) / NOALLOC_PER_BLOCK);
   k_rdot_noalloc<<<grid, NOALLOC_THREADS, 0, st>>>(a, b, n, scratch);
   OST_LAUNCH_CHECK();
   double h = NAN;
-  OST_CUDA(cudaMemcpyAsync(&h, scratch + 8, sizeof(double), cudaMemcpyDeviceToHost, st));
+  OST_CUDA(cudaMemcpyAsync(&h, scratch + NOALLOC_RESULT, sizeof(double), cudaMemcpyDeviceToHost, st));
   OST_CUDA(cudaStreamSynchronize(st));
   return error_code() ? NAN : h;
 }

@@ -1,25 +1,38 @@
 // reduce.cuh -- deterministic single-pass grid reductions.
 //
-// Every block reduces its values with warp shuffles and shared memory, writes
-// one partial per block, and the last block to finish (ticket counter with a
-// device-scope fence) sums the partials in block order.  The grid size only
-// depends on the problem size and the SM count, so results are bitwise
-// reproducible run to run; no floating-point atomics are used.
+// Every block reduces its values with warp shuffles and shared memory and
+// writes one partial per block.  The partials are then summed in two levels
+// inside the same kernel: the last block to finish in each group of
+// RED_GROUP consecutive blocks sums that group's partials (ticket counter
+// per group, device-scope fences), and the last group to finish sums the
+// group totals.  A single last block summing every partial would read them
+// one L2 round trip after another; with 10^4 blocks that tail alone costs
+// tens of microseconds.  All sums run in a fixed order that depends only on
+// the grid size, so results are bitwise reproducible run to run; no
+// floating-point atomics are used.
 #pragma once
 #include "runtime.cuh"
 
 namespace ost {
 
 static constexpr int RED_THREADS = 256;
+static constexpr int RED_GROUP = 64;          // blocks per first-level group
+static constexpr int RED_COUNTERS = 16384;    // ticket counters: [0] final, [1 + g] group g
 
 struct ReduceWs {
-  unsigned int* counter;   // zero between reductions
-  double* partials;        // [NV * max_blocks]
+  unsigned int* counter;   // [RED_COUNTERS], all zero between reductions
+  double* partials;        // [NV * max_blocks] block partials
+  double* gpartials;       // [NV * max_groups] group totals
   int max_blocks;
+  int max_groups;
 };
 
-// Workspace for reductions of up to NV values over at most max_blocks blocks.
+// Workspace for reductions of up to NV values over at most max_blocks blocks
+// (max_blocks <= RED_GROUP * (RED_COUNTERS - 1)).
 ReduceWs reduce_ws(int nv, int max_blocks);
+// Allocates the workspace for reductions with up to `partials` = NV x blocks
+// block partials ahead of a graph capture (nothing may allocate inside one).
+void reduce_ws_reserve(size_t partials);
 
 // Grid for streaming reductions: enough blocks to keep every SM's load
 // queues full (up to 16 blocks of 256 threads per SM), each thread handling a
@@ -57,32 +70,57 @@ OST_D void block_reduce(double v[NV], double* smem /* [NV * 32] */) {
   }
 }
 
-// Called by every thread of every block after computing its local values.
-// Returns true in thread 0 of the last block, with the totals in `tot`.
+// Second and third stage shared by every variant: bv[NV] holds this block's
+// partials in thread 0.  Returns true in thread 0 of the block that finishes
+// last, with the grid totals in tot.  smem must hold NV * 32 doubles and be
+// free for reuse (callers synchronise before the call).
 template <int NV>
-OST_D bool grid_reduce(double v[NV], ReduceWs ws, double tot[NV]) {
-  __shared__ double smem[NV * 32];
-  __shared__ bool am_last;
-  block_reduce<NV>(v, smem);
+OST_D bool grid_finish(const double bv[NV], ReduceWs ws, double tot[NV], double* smem) {
+  __shared__ int stage;   // 1: this block closed its group, 2: it closed the grid
+  const int g = blockIdx.x / RED_GROUP;
+  const int ng = (gridDim.x + RED_GROUP - 1) / RED_GROUP;
+  const int gsize = min(RED_GROUP, int(gridDim.x) - g * RED_GROUP);
   if (threadIdx.x == 0) {
 #pragma unroll
-    for (int k = 0; k < NV; ++k) ws.partials[k * ws.max_blocks + blockIdx.x] = v[k];
+    for (int k = 0; k < NV; ++k) ws.partials[k * ws.max_blocks + blockIdx.x] = bv[k];
     __threadfence();
-    unsigned int t = atomicAdd(ws.counter, 1u);
-    am_last = (t == gridDim.x - 1);
+    const unsigned int t = atomicAdd(ws.counter + 1 + g, 1u);
+    stage = (t == unsigned(gsize - 1)) ? 1 : 0;
   }
   __syncthreads();
-  if (!am_last) return false;
+  if (stage == 0) return false;
   __threadfence();
-  // last block: sum partials in fixed order, one value per warp-strided lane
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
+    double gs[NV];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      const double* src = ws.partials + k * ws.max_blocks + g * RED_GROUP;
+      double a = lane < gsize ? __ldcg(src + lane) : 0.0;
+      if (lane + 32 < gsize) a += __ldcg(src + lane + 32);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+      gs[k] = a;
+    }
+    if (lane == 0) {
+#pragma unroll
+      for (int k = 0; k < NV; ++k) ws.gpartials[k * ws.max_groups + g] = gs[k];
+      ws.counter[1 + g] = 0;
+      __threadfence();
+      const unsigned int t = atomicAdd(ws.counter, 1u);
+      stage = (t == unsigned(ng - 1)) ? 2 : 0;
+    }
+  }
+  __syncthreads();
+  if (stage != 2) return false;
+  __threadfence();
   double s[NV];
 #pragma unroll
   for (int k = 0; k < NV; ++k) s[k] = 0.0;
-  for (int b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
+  for (int i = threadIdx.x; i < ng; i += blockDim.x) {
 #pragma unroll
-    for (int k = 0; k < NV; ++k) s[k] += __ldcg(ws.partials + k * ws.max_blocks + b);
+    for (int k = 0; k < NV; ++k) s[k] += __ldcg(ws.gpartials + k * ws.max_groups + i);
   }
-  __syncthreads();
   block_reduce<NV>(s, smem);
   if (threadIdx.x == 0) {
 #pragma unroll
@@ -93,6 +131,16 @@ OST_D bool grid_reduce(double v[NV], ReduceWs ws, double tot[NV]) {
   return false;
 }
 
+// Called by every thread of every block after computing its local values.
+// Returns true in thread 0 of the last block, with the totals in `tot`.
+template <int NV>
+OST_D bool grid_reduce(double v[NV], ReduceWs ws, double tot[NV]) {
+  __shared__ double smem[NV * 32];
+  block_reduce<NV>(v, smem);
+  __syncthreads();
+  return grid_finish<NV>(v, ws, tot, smem);
+}
+
 // Variant for single-precision solvers: per-thread values and the
 // intra-warp tree in FP32 (GB300 runs FP64 at 1/64 of the FP32 rate, so FP64
 // per-thread accumulation would cost as much as the memory traffic), the
@@ -101,7 +149,6 @@ OST_D bool grid_reduce(double v[NV], ReduceWs ws, double tot[NV]) {
 template <int NV>
 OST_D bool grid_reduce_f32w(float vf[NV], ReduceWs ws, double tot[NV]) {
   __shared__ double smem[NV * 32];
-  __shared__ bool am_last;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int nwarps = (blockDim.x + 31) >> 5;
 #pragma unroll
@@ -114,36 +161,69 @@ OST_D bool grid_reduce_f32w(float vf[NV], ReduceWs ws, double tot[NV]) {
     for (int k = 0; k < NV; ++k) smem[k * 32 + warp] = double(vf[k]);
   }
   __syncthreads();
+  double bv[NV];
   if (threadIdx.x == 0) {
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
       double t = 0.0;
       for (int w = 0; w < nwarps; ++w) t += smem[k * 32 + w];
-      ws.partials[k * ws.max_blocks + blockIdx.x] = t;
+      bv[k] = t;
     }
-    __threadfence();
-    unsigned int t = atomicAdd(ws.counter, 1u);
-    am_last = (t == gridDim.x - 1);
   }
   __syncthreads();
-  if (!am_last) return false;
-  __threadfence();
-  double s[NV];
+  return grid_finish<NV>(bv, ws, tot, smem);
+}
+
+// Per-system reduction for kernels that give each system of a batch its own
+// lane: system k = lane % NSP (NSP a power of two <= 32).  Each thread passes
+// one FP32 value (zero if it has none); returns true in thread 0 of the last
+// block with tot[k] = the sum over all threads of system k.  The intra-warp
+// tree is FP32, the cross-warp and cross-block sums FP64, in a fixed order.
+template <int NSP>
+OST_D bool grid_reduce_lanes(float vf, ReduceWs ws, double tot[NSP]) {
+  __shared__ double smem[NSP * 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nwarps = (blockDim.x + 31) >> 5;
 #pragma unroll
-  for (int k = 0; k < NV; ++k) s[k] = 0.0;
-  for (int b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
-#pragma unroll
-    for (int k = 0; k < NV; ++k) s[k] += __ldcg(ws.partials + k * ws.max_blocks + b);
-  }
+  for (int o = 16; o >= NSP; o >>= 1) vf += __shfl_xor_sync(0xffffffffu, vf, o);
+  if (lane < NSP) smem[lane * 32 + warp] = double(vf);
   __syncthreads();
-  block_reduce<NV>(s, smem);
+  double bv[NSP];
   if (threadIdx.x == 0) {
 #pragma unroll
-    for (int k = 0; k < NV; ++k) tot[k] = s[k];
-    *ws.counter = 0;
-    return true;
+    for (int k = 0; k < NSP; ++k) {
+      double t = 0.0;
+      for (int w = 0; w < nwarps; ++w) t += smem[k * 32 + w];
+      bv[k] = t;
+    }
   }
-  return false;
+  __syncthreads();
+  return grid_finish<NSP>(bv, ws, tot, smem);
+}
+
+// Segmented reduction: the grid's blocks form NSEG consecutive segments of
+// seg_blocks blocks (segment = blockIdx.x / seg_blocks, one system each).
+// Each thread passes one FP32 value; returns true in thread 0 of the last
+// block with tot[k] = the sum over segment k.  FP32 intra-warp, FP64 above.
+template <int NSEG>
+OST_D bool grid_reduce_seg(float vf, int seg_blocks, ReduceWs ws, double tot[NSEG]) {
+  __shared__ double smem[NSEG * 32 > 32 ? NSEG * 32 : 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nwarps = (blockDim.x + 31) >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) vf += __shfl_down_sync(0xffffffffu, vf, o);
+  if (lane == 0) smem[warp] = double(vf);
+  __syncthreads();
+  double bv[NSEG];
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < nwarps; ++w) t += smem[w];
+    const int seg = blockIdx.x / seg_blocks;
+#pragma unroll
+    for (int k = 0; k < NSEG; ++k) bv[k] = (k == seg) ? t : 0.0;
+  }
+  __syncthreads();
+  return grid_finish<NSEG>(bv, ws, tot, smem);
 }
 
 }  // namespace ost
