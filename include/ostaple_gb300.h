@@ -269,6 +269,14 @@ double ker_find_min_eigenvalue_openacc(const su3_soa *u, ferm_param *pars, vec3_
 void find_min_max_eigenvalue_soloopenacc(const su3_soa *u, ferm_param *pars, vec3_soa *loc_r, vec3_soa *loc_h,
                                          vec3_soa *loc_p1, vec3_soa *loc_p2, double *minmax);
 
+/* out = (m^2 + shift) in - D_eo D_oe in computed in double-float arithmetic
+ * (FP32 pairs with error-free transformations, ~1e-14 relative): the
+ * operator of the mixed solvers' intermediate reliable updates, exposed for
+ * testing and for callers that want a near-FP64 M^+M at FP32 speed.  Needs
+ * phases of 0 or pi.  No counterpart in the reference. */
+int ostaple_mdagm_df(const su3_soa *u, const double_soa *phases, double mass, double shift, vec3_soa *out,
+                     const vec3_soa *in);
+
 /* Mixed-precision CG: FP32 iteration, FP64 solution and reliable updates of
  * the residual when |r|^2 < inverter_tricks.mixedPrecisionDelta * max|r|^2
  * (inverter_mixedp.c:41-48).  FP32 links come from ip.u_f when set (the

@@ -122,6 +122,11 @@ def fermion_matrix_multiplication(u, out, inp, temp1, pars: FermParam) -> None:
     check(0, "fermion_matrix_multiplication")
 
 
+def mdagm_df(u, phases, mass: float, out, inp, shift: float = 0.0) -> None:
+    """out = (m^2 + shift) inp - D_eo D_oe inp in double-float arithmetic."""
+    check(lib().ostaple_mdagm_df(ptr(u), ptr(phases), mass, shift, ptr(out), ptr(inp)), "ostaple_mdagm_df")
+
+
 def l2norm2_global(v) -> float:
     r = lib().l2norm2_global(ptr(v))
     check(0, "l2norm2_global")

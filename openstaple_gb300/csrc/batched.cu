@@ -533,7 +533,9 @@ BatchResult batched_mixed_cg(const BatchBuffers& B, const double* m2, double res
         const bool was_done = h.done[k];
         k_b_accumulate<<<8 * rt().num_sms, 256, 0, cs>>>(B.x + k * n, B.xf + k * n, n);
         OST_LAUNCH_CHECK();
-        fp64_mdagm(B, B.t64, B.x + k * n, m2[k], cs);
+        // intermediate reliable updates in double-float, closing residuals in FP64
+        if (!was_done && B.use_df) df_mdagm(B.df, B.dfw, B.t64, B.x + k * n, m2[k], cs);
+        else fp64_mdagm(B, B.t64, B.x + k * n, m2[k], cs);
         const int gr = reduce_grid(n);
         k_b_residual<<<gr, RED_THREADS, 0, cs>>>(B.b + k * n, B.t64, B.r64, B.r + k * n, B.p + k * n, n, sc, k,
                                                  reduce_ws(2, gr), 1);

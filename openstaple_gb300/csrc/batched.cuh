@@ -38,6 +38,9 @@ struct BatchBuffers {
   float2* s;
   float2* xf;
   float2* t;
+  int use_df;               // reliable updates in double-float arithmetic (exact phases only)
+  DfOperator df;
+  DfWork dfw;
 };
 
 struct BatchResult {

@@ -95,12 +95,19 @@ int ostaple_invert_mixed_batch(const su3_soa* u, const double_soa* phases, doubl
   if (!prepare(u64, static_cast<const double*>(ph), &pr, st)) return INVERTER_FAILURE;
   BatchScal* sc = batch_scalars();
   if (!sc) return INVERTER_FAILURE;
+  DfOperator dop{};
+  DfWork dwk{};
+  const int use_df = pr.mode == PH_SIGN8 &&
+                     df_prepare(u64, pr.u32, static_cast<const unsigned char*>(pr.ph), &dop, &dwk, st);
   int ok = 1;
   for (int s0 = 0; s0 < nsys; s0 += BATCH_MAX) {
     const int m = std::min(BATCH_MAX, nsys - s0);
     BatchBuffers B{};
     if (!batch_buffers(m, &B)) return INVERTER_FAILURE;
     B.u64 = u64; B.ph64 = ph; B.u32 = pr.u32; B.ph32 = pr.ph; B.ph32_mode = pr.mode;
+    B.use_df = use_df;
+    B.df = dop;
+    B.dfw = dwk;
     B.x = x + s0 * n;
     B.b = b + s0 * n;
     double m2[BATCH_MAX];
@@ -162,6 +169,10 @@ int ostaple_multishift_batch(const su3_soa* u, const double_soa* phases, double 
   OST_LAUNCH_CHECK();
   BatchScal* sc = batch_scalars();
   if (!sc) return INVERTER_FAILURE;
+  DfOperator dop{};
+  DfWork dwk{};
+  const int use_df = pr.mode == PH_SIGN8 &&
+                     df_prepare(u64, pr.u32, static_cast<const unsigned char*>(pr.ph), &dop, &dwk, st);
   int ok = 1;
   std::vector<int> sys_rhs, sys_shift;
   for (int k = 0; k < order; ++k)
@@ -183,6 +194,9 @@ int ostaple_multishift_batch(const su3_soa* u, const double_soa* phases, double 
     BatchBuffers B{};
     if (!batch_buffers(m, &B)) return INVERTER_FAILURE;
     B.u64 = u64; B.ph64 = ph; B.u32 = pr.u32; B.ph32 = pr.ph; B.ph32_mode = pr.mode;
+    B.use_df = use_df;
+    B.df = dop;
+    B.dfw = dwk;
     B.x = sx;
     B.b = sb;
     BatchResult rb = batched_mixed_cg(B, m2, res, max_iter, delta_frac > 0 ? delta_frac : 1e-4, sc, st);

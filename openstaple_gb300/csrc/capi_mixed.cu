@@ -61,6 +61,14 @@ bool prepare_f32(const Z* u64, const void* u_f, const double* ph64, PreparedF32*
   return error_code() == 0;
 }
 
+// Double-float operator for the reliable updates: the lo parts of the
+// compact links and four work fields.  Only with exact phases (sign bytes)
+// and the library's own compact FP32 links.
+bool prepare_df(const Z* u64, const PreparedF32& pf, DfOperator* op, DfWork* w, cudaStream_t st) {
+  if (pf.mode != PH_SIGN8 || !pf.compact) return false;
+  return df_prepare(u64, pf.u32, static_cast<const unsigned char*>(pf.ph), op, w, st);
+}
+
 template <typename T>
 T* ws_vec(int slot, int k, int nvec) {
   const size_t n = 3 * size_t(rt().g.sizeh);
@@ -104,6 +112,7 @@ int inverter_mixed_precision(inverter_package ip, ferm_param* pars, vec3_soa* so
   B.u32_compact = pf.compact;
   B.ph32 = pf.ph;
   B.ph32_mode = pf.mode;
+  B.use_df = prepare_df(B.u64, pf, &B.df, &B.dfw, st) ? 1 : 0;
   MixedOptions o;
   o.mass2 = pars->ferm_mass * pars->ferm_mass + shift;
   o.res = res;
@@ -148,6 +157,7 @@ int ostaple_invert_mixed(const su3_soa* u, const double_soa* phases, double mass
   B.u32_compact = pf.compact;
   B.ph32 = pf.ph;
   B.ph32_mode = pf.mode;
+  B.use_df = prepare_df(B.u64, pf, &B.df, &B.dfw, st) ? 1 : 0;
   MixedOptions o;
   o.mass2 = mass * mass + shift;
   o.res = res;
@@ -201,6 +211,28 @@ int ostaple_time_kernel(int which, const su3_soa* u, const double_soa* phases, i
     *ms = double(t) / reps;
     return error_code();
   }
+  if (which == 3) {   // double-float M^+M (split + D_oe + D_eo)
+    PreparedF32 pf;
+    if (!prepare_f32(u64, nullptr, static_cast<const double*>(ph), &pf, st)) return -4;
+    DfOperator op;
+    DfWork w;
+    if (!prepare_df(u64, pf, &op, &w, st)) return -12;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float t = 0;
+    for (int pass = 0; pass < 2; ++pass) {
+      cudaEventRecord(e0, st);
+      for (int k = 0; k < reps; ++k) df_mdagm(op, w, a, b, 0.01, st);
+      cudaEventRecord(e1, st);
+      cudaEventSynchronize(e1);
+      cudaEventElapsedTime(&t, e0, e1);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *ms = double(t) / reps;
+    return error_code();
+  }
   MixedBuffers B{};
   B.u64 = u64;
   B.ph64 = ph;
@@ -217,6 +249,28 @@ int ostaple_time_kernel(int which, const su3_soa* u, const double_soa* phases, i
   B.ph32_mode = pf.mode;
   MixScal* sc = mix_scalars();
   *ms = time_mixed_kernel(B, sc + 1, which, reps, st);
+  return error_code();
+}
+
+int ostaple_mdagm_df(const su3_soa* u, const double_soa* phases, double mass, double shift, vec3_soa* out,
+                     const vec3_soa* in) {
+  if (!require_init("ostaple_mdagm_df")) return -2;
+  cudaStream_t st = rt().stream;
+  const Z* u64 = dev(reinterpret_cast<const Z*>(u), "u");
+  const void* ph = resolve(phases, "phases");
+  const Z* din = dev(reinterpret_cast<const Z*>(in), "in");
+  Z* dout = dev(reinterpret_cast<Z*>(out), "out");
+  if (!u64 || !ph || !din || !dout) return -3;
+  PreparedF32 pf;
+  if (!prepare_f32(u64, nullptr, static_cast<const double*>(ph), &pf, st)) return -4;
+  DfOperator op;
+  DfWork w;
+  if (!prepare_df(u64, pf, &op, &w, st)) {
+    set_error(-12, "ostaple_mdagm_df: phases must be 0 or pi (staggered phases and boundary signs)");
+    return -12;
+  }
+  df_mdagm(op, w, dout, din, mass * mass + shift, st);
+  OST_CUDA(cudaStreamSynchronize(st));
   return error_code();
 }
 

@@ -1,0 +1,49 @@
+// dslash_df.cuh -- M^+M in double-float arithmetic: every FP64 number is
+// carried as an unevaluated sum hi + lo of two FP32 numbers (about 48
+// significant bits) and products and sums use error-free transformations
+// (Dekker's product via FMA, Knuth's two-sum; Dekker 1971, Knuth TAOCP vol. 2
+// 4.2.2).  GB300 executes FP64 at 1/62 of its FP32 rate and the FP64 Dslash
+// is bound by that rate (0.42 ms per half application at 32^4, 96% of the
+// FP64 peak); in double-float the same operator becomes memory bound.  The
+// mixed-precision solvers use it for their intermediate reliable updates,
+// where a relative accuracy of ~1e-14 is ample; every final (true) residual
+// is still computed in native FP64.
+#pragma once
+#include <cuda_runtime.h>
+#include "common.cuh"
+
+namespace ost {
+
+// Double-float operand set for D_eo / D_oe: links split into FP32 hi and lo
+// parts (rows 0-1, compact layout [dir][6][sizeh]) and one sign byte per link.
+struct DfOperator {
+  const float2* u_hi;
+  const float2* u_lo;
+  const unsigned char* signs;
+};
+
+// Work fields of one double-float M^+M application: the input and the
+// odd-parity intermediate in hi/lo form (3*sizeh complex each).
+struct DfWork {
+  float2* x_hi;
+  float2* x_lo;
+  float2* t_hi;
+  float2* t_lo;
+};
+
+// lo parts of the compact links: lo = (float)(u - (double)(float)u), the hi
+// parts being the existing compact FP32 copy.
+void links_to_lo_compact(const double2* u64, float2* u_lo, long sizeh, cudaStream_t st);
+
+// Operator and work fields for a solve on the current lattice: computes the
+// lo link parts from the FP64 links (workspace slots WS_LINKS_LO and WS_DF).
+// u_hi: the compact FP32 links (hi parts), signs: one sign byte per link.
+bool df_prepare(const double2* u64, const float2* u_hi, const unsigned char* signs, DfOperator* op, DfWork* w,
+                cudaStream_t st);
+
+// out = (m2 + shift) in - D_eo D_oe in, in double-float arithmetic; in and
+// out are FP64 vec3 fields on the even sites.  Needs exact phases (signs).
+void df_mdagm(const DfOperator& op, const DfWork& w, double2* out, const double2* in, double m2,
+              cudaStream_t st);
+
+}  // namespace ost

@@ -352,7 +352,10 @@ MixedResult mixed_cg(const MixedBuffers& B, const MixedOptions& o, MixScal* sc, 
     if (h.need_rel) {
       k_mx_accumulate<<<8 * rt().num_sms, 256, 0, cs>>>(B.x, B.xf, n);
       OST_LAUNCH_CHECK();
-      fp64_mdagm(B, B.t64, B.x, B.t64b, o.mass2, cs);
+      // an intermediate reliable update needs ~1e-14 relative accuracy:
+      // double-float suffices; the closing residual below stays in FP64
+      if (B.use_df) df_mdagm(B.df, B.dfw, B.t64, B.x, o.mass2, cs);
+      else fp64_mdagm(B, B.t64, B.x, B.t64b, o.mass2, cs);
       int gr = reduce_grid(n);
       k_mx_residual<<<gr, RED_THREADS, 0, cs>>>(B.b, B.t64, B.r64, B.r, B.p, n, sc, reduce_ws(2, gr), 1);
       OST_LAUNCH_CHECK();

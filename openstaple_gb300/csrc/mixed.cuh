@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include "common.cuh"
+#include "dslash_df.cuh"
 
 namespace ost {
 
@@ -63,6 +64,9 @@ struct MixedBuffers {
   float2* s;
   float2* xf;
   float2* t;               // odd-parity temporary
+  int use_df;              // reliable updates in double-float arithmetic (exact phases only)
+  DfOperator df;
+  DfWork dfw;
 };
 
 // Converts the first two rows of FP64 su3_soa[8] links to a compact FP32 copy.

@@ -76,6 +76,8 @@ enum WorkspaceSlot {
   WS_CGM,          // batched multi-shift scalars
   WS_BATCH,        // batched solver vectors
   WS_BATCH64,
+  WS_LINKS_LO,     // lo parts of the double-float links
+  WS_DF,           // double-float M^+M work fields
   WS_NSLOTS
 };
 

@@ -111,6 +111,7 @@ SIGNATURES = {
     "scal_prod_global_ri": (None, [_P, _P, C.POINTER(_D)]),
     "real_scal_prod_global": (_D, [_P, _P]),
     "l2norm2_global": (_D, [_P]),
+    "ostaple_mdagm_df": (_I, [_P, _P, _D, _D, _P, _P]),
     "ostaple_real_scal_prod_global_noalloc": (_D, [_P, _P]),
     "combine_in1xfactor_plus_in2": (None, [_P, _D, _P, _P]),
     "multiply_fermion_x_doublefactor": (None, [_P, _D]),

@@ -114,3 +114,36 @@ def test_unregistered_host_pointer_is_an_error(lat_factory):
     out = np.zeros_like(v)
     with pytest.raises(RuntimeError, match="neither registered"):
         api.acc_Deo(u, out, v, ph)
+
+
+@pytest.mark.parametrize("dims", [(4, 4, 4, 4), (8, 8, 8, 8), (4, 6, 8, 10)])
+def test_double_float_mdagm_matches_fp64(lat_factory, dims):
+    """M^+M in double-float arithmetic (the operator of the mixed solvers'
+    intermediate reliable updates) against the FP64 oracle: 1e-13 relative,
+    the FP64 Dslash tolerance; in practice ~1e-14."""
+    from oracle import Oracle
+    o = Oracle(dims)
+    lat = lat_factory(dims)
+    u = F.random_su3_links(dims, 31)
+    v = F.gaussian_vec3(dims, 32)
+    ph = F.staggered_phases(dims)
+    out = lat.vec3()
+    for a in (u, v, ph, out):
+        lat.present(a)
+    for mass, shift in ((0.05, 0.0), (0.01, 0.37)):
+        api.mdagm_df(u, ph, mass, out, v, shift)
+        lat.update_host(out)
+        assert relerr(out, o.mdagm(u, v, ph, mass * mass + shift)) <= TOL
+
+
+def test_double_float_mdagm_needs_exact_phases(lat_factory):
+    dims = (4, 4, 4, 4)
+    lat = lat_factory(dims)
+    u = F.random_su3_links(dims, 33)
+    v = F.gaussian_vec3(dims, 34)
+    ph = F.staggered_phases(dims, 0.3)
+    out = lat.vec3()
+    for a in (u, v, ph, out):
+        lat.present(a)
+    with pytest.raises(RuntimeError, match="phases must be 0 or pi"):
+        api.mdagm_df(u, ph, 0.05, out, v)
