@@ -482,9 +482,14 @@ BatchResult batched_mixed_cg(const BatchBuffers& B, const double* m2, double res
   init.nsys = NSY;
   for (int k = 0; k < NSY; ++k) init.m2[k] = m2[k];
   OST_CUDA(cudaMemcpyAsync(sc, &init, sizeof(BatchScal), cudaMemcpyHostToDevice, cs));
-  for (int k = 0; k < NSY; ++k) blas_norm2<double>(B.b + k * n, n, &sc->bnorm2[k], cs);
+  for (int k = 0; k < NSY; ++k) {
+    blas_norm2<double>(B.b + k * n, n, &sc->bnorm2[k], cs);
+    blas_norm2<double>(B.x + k * n, n, &sc->true_r2[k], cs);   // |x0|^2, overwritten below
+  }
   OST_CUDA(cudaMemcpyAsync(g_bhost, sc, sizeof(BatchScal), cudaMemcpyDeviceToHost, cs));
   OST_CUDA(cudaStreamSynchronize(cs));
+  bool zero_guess[BATCH_MAX];
+  for (int k = 0; k < NSY; ++k) zero_guess[k] = g_bhost->true_r2[k] == 0.0;
   double bn[BATCH_MAX], fp32_target[BATCH_MAX];
   for (int k = 0; k < NSY; ++k) {
     bn[k] = g_bhost->bnorm2[k];
@@ -495,7 +500,9 @@ BatchResult batched_mixed_cg(const BatchBuffers& B, const double* m2, double res
   OST_CUDA(cudaMemcpyAsync(sc, &init, sizeof(BatchScal), cudaMemcpyHostToDevice, cs));
   blas_zero<float>(B.xf, NSY * n, cs);
   for (int k = 0; k < NSY; ++k) {
-    fp64_mdagm(B, B.t64, B.x + k * n, m2[k], cs);
+    // r0 = b - A x0; a zero guess needs no operator application
+    if (zero_guess[k]) OST_CUDA(cudaMemsetAsync(B.t64, 0, n * sizeof(double2), cs));
+    else fp64_mdagm(B, B.t64, B.x + k * n, m2[k], cs);
     const int gr = reduce_grid(n);
     k_b_residual<<<gr, RED_THREADS, 0, cs>>>(B.b + k * n, B.t64, B.r64, B.r + k * n, B.p + k * n, n, sc, k,
                                              reduce_ws(2, gr), 0);

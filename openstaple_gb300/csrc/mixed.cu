@@ -300,15 +300,19 @@ MixedResult mixed_cg(const MixedBuffers& B, const MixedOptions& o, MixScal* sc, 
   init.every = o.reliable_every;
   OST_CUDA(cudaMemcpyAsync(sc, &init, sizeof(MixScal), cudaMemcpyHostToDevice, cs));
   blas_norm2<double>(B.b, n, &sc->bnorm2, cs);
+  blas_norm2<double>(B.x, n, &sc->true_r2, cs);     // |x0|^2, overwritten below
   OST_CUDA(cudaMemcpyAsync(g_host, sc, sizeof(MixScal), cudaMemcpyDeviceToHost, cs));
   OST_CUDA(cudaStreamSynchronize(cs));
   const double bn = g_host->bnorm2;
+  const bool zero_guess = g_host->true_r2 == 0.0;
   double fp32_target = o.safety * o.res;
   init.target2 = fp32_target * fp32_target * bn;
   init.bnorm2 = bn;
   OST_CUDA(cudaMemcpyAsync(sc, &init, sizeof(MixScal), cudaMemcpyHostToDevice, cs));
   blas_zero<float>(B.xf, n, cs);
-  fp64_mdagm(B, B.t64, B.x, B.t64b, o.mass2, cs);
+  // r0 = b - A x0; a zero guess (the usual start) needs no operator application
+  if (zero_guess) OST_CUDA(cudaMemsetAsync(B.t64, 0, n * sizeof(double2), cs));
+  else fp64_mdagm(B, B.t64, B.x, B.t64b, o.mass2, cs);
   {
     int gr = reduce_grid(n);
     k_mx_residual<<<gr, RED_THREADS, 0, cs>>>(B.b, B.t64, B.r64, B.r, B.p, n, sc, reduce_ws(2, gr), 0);
