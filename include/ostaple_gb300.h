@@ -255,6 +255,21 @@ int multishift_invert(const su3_soa *u, ferm_param *pars, RationalApprox *approx
                       vec3_soa *loc_s, vec3_soa *loc_p, vec3_soa *shiftferm, const int max_cg,
                       int *cg_return);
 /* out = a0 in + sum_i a_i in_shifted[i] (inverter_multishift_full.h:30-33) */
+/* Rational approximations r(x) = a0 + sum_i a_i/(x + b_i) (rationalapprox.h:29-53):
+ * .REMEZ file names, reading and writing, rescaling of a mother
+ * approximation on [lambda_min, 1] to the measured spectrum [min, max] of
+ * M^+M (x -> x/(1.05 max)), the inverse renormalisation, and evaluation.
+ * Host functions, exported as weak symbols so that a host program that
+ * links the reference's rationalapprox.c keeps its own. */
+char *rational_approx_filename(double error, int exponent_num, int exponent_den, double lambda_min);
+char *rational_approx_filename_old(int approx_order, int exponent_num, int exponent_den, double lambda_min);
+int rationalapprox_read(RationalApprox *rational_approx);
+int rationalapprox_read_custom_nomefile(RationalApprox *rational_approx, char *nomefile);
+void rationalapprox_save(const char *nomefile, RationalApprox *rational_approx);
+void rescale_rational_approximation(RationalApprox *in, RationalApprox *out, double *minmax);
+void renormalize_rational_approximation(RationalApprox *in, RationalApprox *out);
+double rational_approx_evaluate(RationalApprox *in, double x);
+
 void recombine_shifted_vec3_to_vec3(const vec3_soa *in_shifted, const vec3_soa *in, vec3_soa *out,
                                     const RationalApprox *approx);
 

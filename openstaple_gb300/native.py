@@ -132,6 +132,14 @@ SIGNATURES = {
                                _P, _I, C.POINTER(_I)]),
     "recombine_shifted_vec3_to_vec3": (None, [_P, _P, _P, C.POINTER(RationalApprox)]),
     "ker_find_max_eigenvalue_openacc": (_D, [_P, C.POINTER(FermParam), _P, _P, _P]),
+    "rational_approx_filename": (C.c_void_p, [_D, _I, _I, _D]),
+    "rational_approx_filename_old": (C.c_void_p, [_I, _I, _I, _D]),
+    "rationalapprox_read": (_I, [C.POINTER(RationalApprox)]),
+    "rationalapprox_read_custom_nomefile": (_I, [C.POINTER(RationalApprox), C.c_char_p]),
+    "rationalapprox_save": (None, [C.c_char_p, C.POINTER(RationalApprox)]),
+    "rescale_rational_approximation": (None, [C.POINTER(RationalApprox), C.POINTER(RationalApprox), _P]),
+    "renormalize_rational_approximation": (None, [C.POINTER(RationalApprox), C.POINTER(RationalApprox)]),
+    "rational_approx_evaluate": (_D, [C.POINTER(RationalApprox), _D]),
     "ker_find_min_eigenvalue_openacc": (_D, [_P, C.POINTER(FermParam), _P, _P, _P, _D]),
     "find_min_max_eigenvalue_soloopenacc": (None, [_P, C.POINTER(FermParam), _P, _P, _P, _P, _P]),
     "inverter_mixed_precision": (_I, [InverterPackage, C.POINTER(FermParam), _P, _P, _D, _I, _D, C.POINTER(_I)]),

@@ -202,6 +202,12 @@ class Reference:
         "ref_cgm": (_I, [_P, _P, _D, _I, _D, _P, _P, _P, _P, _D, _I, C.POINTER(_I)]),
         "ref_recombine": (None, [_P, _P, _P, _I, _D, _P]),
         "ref_find_min_max": (None, [_P, _P, _D, _P, _P, _P]),
+        "ref_ra_read": (_I, [C.c_char_p, _P]),
+        "ref_ra_save": (None, [C.c_char_p, _P]),
+        "ref_ra_rescale": (None, [_P, _P, _P]),
+        "ref_ra_renormalize": (None, [_P, _P]),
+        "ref_ra_evaluate": (_D, [_P, _D]),
+        "ref_ra_filename": (None, [_D, _I, _I, _D, _P]),
         "ref_find_min": (_D, [_P, _P, _D, _P, _P, _D]),
         "ref_stout_isotropic": (None, [_P, _P, _D]),
         "ref_staples": (None, [_P, _P]),

@@ -32,6 +32,7 @@
 #include "./inverter_multishift_full.h"
 #include "./inverter_package.h"
 #include "./find_min_max.h"
+#include "../RationalApprox/rationalapprox.h"
 #include "./stouting.h"
 #include "./fermion_force.h"
 #include "./fermion_force_utilities.h"
@@ -175,6 +176,18 @@ double ref_find_min(const double *u, double *ph, double mass, double *p, double 
   double mn = ker_find_min_eigenvalue_openacc((su3_soa *)u, &fp, (vec3_soa *)r, h, (vec3_soa *)p, max);
   free(h);
   return mn;
+}
+
+/* ---- rational approximations (rationalapprox.c:83-236) ---- */
+int ref_ra_read(const char *path, RationalApprox *ra) { return rationalapprox_read_custom_nomefile(ra, (char *)path); }
+void ref_ra_save(const char *path, RationalApprox *ra) { rationalapprox_save(path, ra); }
+void ref_ra_rescale(RationalApprox *in, RationalApprox *out, double *minmax) { rescale_rational_approximation(in, out, minmax); }
+void ref_ra_renormalize(RationalApprox *in, RationalApprox *out) { renormalize_rational_approximation(in, out); }
+double ref_ra_evaluate(RationalApprox *in, double x) { return rational_approx_evaluate(in, x); }
+void ref_ra_filename(double error, int num, int den, double lmin, char *out64)
+{
+  char *n = rational_approx_filename(error, num, den, lmin);
+  strncpy(out64, n, 63); out64[63] = 0; free(n);
 }
 
 /* ---- multi-shift CG (inverter_multishift_full.c:23-252) ---- */
