@@ -40,7 +40,8 @@ PROFILE_TRAFFIC = ROOT / "profiles" / "traffic.json"
 FALLBACK_HBM = 6800.0
 
 # algorithmic bytes per output site of one hop application
-BYTES_F32_SIGN = 8 * 12 * 4 + 8 * 1 + 3 * 8 + 3 * 8      # links(2 rows) + sign bytes + in + out = 440
+# D_oe of the mixed solver per output site: links (2 rows FP32) + sign bytes + r and p_old in + p_new and t out
+BYTES_F32_SIGN = 8 * 12 * 4 + 8 * 1 + 2 * 3 * 8 + 2 * 3 * 8   # = 488
 BYTES_F64_ANGLE = 8 * 12 * 8 + 8 * 8 + 3 * 16 + 3 * 16   # links(2 rows) + angles + in + out = 928
 
 
@@ -58,9 +59,23 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--skip-fp64", action="store_true", help="skip the plain FP64 CG arm (profiling runs)")
+    ap.add_argument("--rhs", type=int, default=1,
+                    help="right-hand sides per step; >1 solves them together with the batched solver")
     ap.add_argument("--delta", type=float, default=1e-4,
                     help="reliable update when |r|^2 < delta * max|r|^2 since the last one")
     return ap.parse_args()
+
+
+def max_over_ranks(v: float, world: int, device: str = "cuda") -> float:
+    """The slowest rank's time: a step of the job ends when every replica has
+    finished (all_reduce MAX over the default process group)."""
+    if world <= 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
 
 
 def peaks():
@@ -209,7 +224,13 @@ def main():
     x = lat.vec3()
     for a in (u, ph, b, x):
         lat.present(a)
-    zero = np.zeros_like(x)
+    nrhs = max(1, args.rhs)
+    if nrhs > 1:     # several right-hand sides: seeded sources, one batched solve per step
+        from openstaple_gb300 import fields as F
+        bs = np.stack([b] + [F.gaussian_vec3(dims, args.seed + 17 * rank + 100 + k) for k in range(nrhs - 1)])
+        xs = lat.vec3(nrhs)
+        lat.present(bs)
+        lat.present(xs)
 
     def barrier():
         if world > 1:
@@ -221,7 +242,7 @@ def main():
     for a in work:
         lat.present(a, copy=False)
     fp = api.make_ferm_param(args.mass, ph)
-    fp64 = {"ms": float("nan"), "iters": 0, "status": -1}
+    fp64 = {"ms": None, "iters": 0, "status": -1}
     for k in range(0 if args.skip_fp64 else 2):
         L.set_vec3_soa_to_zero(x.ctypes.data)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -235,8 +256,38 @@ def main():
         lat.release(a)
 
     def solve():
+        if nrhs > 1:
+            for k in range(nrhs):
+                L.set_vec3_soa_to_zero(xs[k].ctypes.data)
+            r = api.invert_mixed_batch(u, ph, args.mass, xs, bs, None, args.res, 100000, args.delta)
+            return dict(status=r["status"], iters=int(r["iters"].max()), true_res=float(r["true_res"].max()),
+                        n_reliable=int(r["n_reliable"].max()))
         L.set_vec3_soa_to_zero(x.ctypes.data)
         return api.invert_mixed(u, ph, args.mass, 0.0, x, b, args.res, 100000, 0, args.delta)
+
+    # the same workload with 4 right-hand sides solved together (reported beside the headline)
+    batched4 = None
+    if nrhs == 1 and not args.skip_fp64:
+        from openstaple_gb300 import fields as F
+        b4 = np.stack([b] + [F.gaussian_vec3(dims, args.seed + 17 * rank + 100 + k) for k in range(3)])
+        x4 = lat.vec3(4)
+        lat.present(b4)
+        lat.present(x4)
+        t4 = []
+        for k in range(2):
+            x4[...] = 0
+            lat.update_device(x4)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record(stream)
+            r4 = api.invert_mixed_batch(u, ph, args.mass, x4, b4, None, args.res, 100000, args.delta)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            t4.append(e0.elapsed_time(e1))
+        batched4 = {"ms_per_solve": min(t4) / 4, "status": int(r4["status"]),
+                    "true_residual_max": float(r4["true_res"].max())}
+        lat.release(b4)
+        lat.release(x4)
 
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clk:
@@ -249,12 +300,8 @@ def main():
         e1.record(stream)
         barrier()
     launches = L.ostaple_kernel_launches() - launches0
-    ms = e0.elapsed_time(e1) / args.steps
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * 1e3 / ms
+    ms = max_over_ranks(e0.elapsed_time(e1) / args.steps, world)
+    value = world * nrhs * 1e3 / ms
     ok = all(i["status"] == 1 and i["true_res"] <= args.res for i in infos)
 
     # roofline of the dominant kernel (the FP32 hop of the mixed solver), timed alone
@@ -277,28 +324,28 @@ def main():
     # end to end through the C entry points with pinned host buffers
     e2e = None
     if not args.no_e2e:
-        for a in (u, ph, b, x):
+        xe, be = (xs, bs) if nrhs > 1 else (x, b)
+        for a in (u, ph, be, xe):
             L.ostaple_pin_host(a.ctypes.data, a.nbytes)
-        h2d = u.nbytes + ph.nbytes + b.nbytes + x.nbytes
-        d2h = x.nbytes
+        h2d = u.nbytes + ph.nbytes + be.nbytes + xe.nbytes
+        d2h = xe.nbytes
         times = []
         for k in range(args.warmup + args.steps):
-            x[...] = zero
+            xe[...] = 0
             barrier()
             t0 = time.perf_counter()
-            for a in (u, ph, b, x):
+            for a in (u, ph, be, xe):
                 lat.update_device(a)
-            api.invert_mixed(u, ph, args.mass, 0.0, x, b, args.res, 100000, 0, args.delta)
-            lat.update_host(x)
+            if nrhs > 1:
+                api.invert_mixed_batch(u, ph, args.mass, xe, be, None, args.res, 100000, args.delta)
+            else:
+                api.invert_mixed(u, ph, args.mass, 0.0, xe, be, args.res, 100000, 0, args.delta)
+            lat.update_host(xe)
             dt = time.perf_counter() - t0
             if k >= args.warmup:
                 times.append(dt)
-        e2e_ms = 1e3 * float(np.mean(times))
-        if world > 1:
-            t = torch.tensor([e2e_ms], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            e2e_ms = float(t.item())
-        e2e = {"value": world * 1e3 / e2e_ms, "unit": "solves/s", "ms_per_step": e2e_ms,
+        e2e_ms = max_over_ranks(1e3 * float(np.mean(times)), world)
+        e2e = {"value": world * nrhs * 1e3 / e2e_ms, "unit": "solves/s", "ms_per_step": e2e_ms,
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)}
 
     cpu = None
@@ -313,14 +360,18 @@ def main():
             "data": "synthetic (seeded exp(i*0.3*H) links, Gaussian source)",
             "config": {"workload": f"MdagM solve {'x'.join(map(str, dims))} m={args.mass} to FP64 true residual "
                                    f"{args.res}",
-                       "solver": "mixed-precision CG (FP32 iteration, FP64 reliable updates, CUDA-graph chunks)",
+                       "solver": ("mixed-precision CG (FP32 iteration, double-float reliable updates, FP64 final "
+                                  "residual, CUDA-graph chunks)" if nrhs == 1 else
+                                  f"batched mixed-precision CG, {nrhs} right-hand sides sharing each link load"),
+                       "rhs_per_step": nrhs,
+                       "batched_4rhs": batched4,
                        "iterations": infos[-1]["iters"], "reliable_updates": infos[-1]["n_reliable"],
                        "true_residual": infos[-1]["true_res"], "all_converged": ok,
                        "plain_fp64_cg": {"ms": fp64["ms"], "iterations": fp64["iters"], "status": fp64["status"]},
-                       "speedup_vs_plain_fp64_cg": fp64["ms"] / ms,
+                       "speedup_vs_plain_fp64_cg": fp64["ms"] * nrhs / ms if fp64["ms"] else None,
                        "l2": "inputs larger than L2 (FP32 links 201 MB, FP64 links 604 MB > 129 MB)",
                        "parallelism": f"replicas x{world}"},
-            "roofline": {"kernel": "k_mx_doe (FP32 D_oe, compact links + sign bytes)", "bound": "hbm",
+            "roofline": {"kernel": "k_mx_doe (FP32 D_oe with the direction update, compact links + sign bytes)", "bound": "hbm",
                          "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                          "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
                          "traffic": traffic, "bytes_per_site": BYTES_F32_SIGN, "ms_per_launch": kms.value},
