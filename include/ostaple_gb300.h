@@ -388,6 +388,17 @@ int ostaple_multishift_batch(const su3_soa *u, const double_soa *phases, double 
  * (FP32 accumulation).  Weights are FP32 masters, 4*64*8 floats, row-major
  * [layer][hop*8 + in_channel][out_channel].  Phases must be 0 or pi. */
 int ostaple_net_init(unsigned seed, double scale);                 /* uniform in [-scale, scale] */
+/* Weight files (host only, no GPU needed): magic "OSTNETWT", version 1,
+ * shape 4x64x8, FP32 weights, FNV-1a 64-bit checksum of header and weights.
+ * Load returns -17 (cannot open), -18 (truncated, wrong magic, version or
+ * shape) or -19 (checksum mismatch) and leaves w untouched on error. */
+int ostaple_net_weights_save(const char *path, const float *w);
+int ostaple_net_weights_load(const char *path, float *w);
+/* Failure-path self-test of the tensor-core kernels' bounded mbarrier wait:
+ * with signal = 0 nothing arrives, the wait gives up after its poll limit,
+ * the error word is set and -13 is returned (error state set, the context
+ * stays usable); with signal = 1 it completes and 0 is returned. */
+int ostaple_selftest_bounded_wait(int signal);
 int ostaple_net_set_weights(const float *w);
 int ostaple_net_get_weights(float *w);
 /* out = N(in), in/out FP64 vec3_soa on even sites (computed in BF16/FP32) */

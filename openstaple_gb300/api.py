@@ -316,6 +316,17 @@ def net_get_weights() -> np.ndarray:
     return w
 
 
+def net_weights_save(path, w: np.ndarray) -> None:
+    w = np.ascontiguousarray(w, dtype=np.float32).reshape(NET_SHAPE)
+    check(lib().ostaple_net_weights_save(str(path).encode(), w.ctypes.data), "ostaple_net_weights_save")
+
+
+def net_weights_load(path) -> np.ndarray:
+    w = np.zeros(NET_SHAPE, np.float32)
+    check(lib().ostaple_net_weights_load(str(path).encode(), w.ctypes.data), "ostaple_net_weights_load")
+    return w
+
+
 def net_apply(u, phases, inp, out) -> None:
     check(lib().ostaple_net_apply(ptr(u), ptr(phases), ptr(inp), ptr(out)), "ostaple_net_apply")
 

@@ -490,6 +490,10 @@ BatchResult batched_mixed_cg(const BatchBuffers& B, const double* m2, double res
   OST_CUDA(cudaStreamSynchronize(cs));
   bool zero_guess[BATCH_MAX];
   for (int k = 0; k < NSY; ++k) zero_guess[k] = g_bhost->true_r2[k] == 0.0;
+  // a system with a non-finite source or guess cannot converge: it is
+  // reported as failed at once and kept out of the iteration
+  bool bad[BATCH_MAX];
+  for (int k = 0; k < NSY; ++k) bad[k] = !std::isfinite(g_bhost->bnorm2[k]) || !std::isfinite(g_bhost->true_r2[k]);
   double bn[BATCH_MAX], fp32_target[BATCH_MAX];
   for (int k = 0; k < NSY; ++k) {
     bn[k] = g_bhost->bnorm2[k];
@@ -508,6 +512,14 @@ BatchResult batched_mixed_cg(const BatchBuffers& B, const double* m2, double res
                                              reduce_ws(2, gr), 0);
     OST_LAUNCH_CHECK();
   }
+  bool finished[BATCH_MAX] = {false};
+  for (int k = 0; k < NSY; ++k) {
+    if (!bad[k]) continue;
+    const int one = 1;
+    OST_CUDA(cudaMemcpyAsync(&sc->done[k], &one, sizeof(int), cudaMemcpyHostToDevice, cs));
+    out.true_res[k] = NAN;
+    finished[k] = true;
+  }
   const int chunk = 8;
   if (!g_bgraph.exec || g_bgraph.sc != sc || g_bgraph.chunk != chunk || g_bgraph.key.nsys != B.nsys ||
       g_bgraph.key.p != B.p || g_bgraph.key.r != B.r || g_bgraph.key.s != B.s || g_bgraph.key.t != B.t ||
@@ -525,7 +537,6 @@ BatchResult batched_mixed_cg(const BatchBuffers& B, const double* m2, double res
     g_bgraph.chunk = chunk;
     g_bgraph.epoch = runtime_epoch();
   }
-  bool finished[BATCH_MAX] = {false};
   for (int guard = 0; guard < 1000000; ++guard) {
     if (error_code()) break;
     OST_CUDA(cudaGraphLaunch(g_bgraph.exec, cs));

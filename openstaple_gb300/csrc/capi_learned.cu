@@ -3,6 +3,7 @@
 // (source, solution) pairs, and flexible CG preconditioned by the network.
 #include <cmath>
 #include <cstdio>
+#include <cstdint>
 #include <cstring>
 #include <vector>
 #include "dslash.cuh"
@@ -202,6 +203,89 @@ void pair_grad(const Prep& p, const float2* b32, const float2* x32, double scale
 }  // namespace
 
 extern "C" {
+
+int ostaple_selftest_bounded_wait(int signal) {
+  if (!require_init("ostaple_selftest_bounded_wait")) return -2;
+  if (!ensure_net()) return -5;
+  net_wait_selftest(g_net.nb, signal ? 1 : 0, 1024, rt().stream);
+  return check_err("ostaple_selftest_bounded_wait") ? 0 : -13;
+}
+
+// ---- weight files: magic, version, shape, FP32 weights, FNV-1a 64 checksum ----
+namespace {
+constexpr char kNetMagic[8] = {'O', 'S', 'T', 'N', 'E', 'T', 'W', 'T'};
+constexpr uint32_t kNetVersion = 1;
+
+uint64_t fnv1a64(const unsigned char* p, size_t n, uint64_t h = 0xcbf29ce484222325ull) {
+  for (size_t i = 0; i < n; ++i) {
+    h ^= p[i];
+    h *= 0x100000001b3ull;
+  }
+  return h;
+}
+
+struct NetFileHeader {
+  char magic[8];
+  uint32_t version, layers, rows, cols;
+};
+}  // namespace
+
+int ostaple_net_weights_save(const char* path, const float* w) {
+  NetFileHeader h;
+  memcpy(h.magic, kNetMagic, 8);
+  h.version = kNetVersion;
+  h.layers = NET_LAYERS;
+  h.rows = NET_K;
+  h.cols = NET_C;
+  const size_t nw = size_t(NET_LAYERS) * NET_K * NET_C;
+  uint64_t sum = fnv1a64(reinterpret_cast<const unsigned char*>(&h), sizeof(h));
+  sum = fnv1a64(reinterpret_cast<const unsigned char*>(w), nw * sizeof(float), sum);
+  FILE* f = fopen(path, "wb");
+  if (!f) {
+    set_error(-17, "ostaple_net_weights_save: cannot open %s", path);
+    return -17;
+  }
+  const bool ok = fwrite(&h, sizeof(h), 1, f) == 1 && fwrite(w, sizeof(float), nw, f) == nw &&
+                  fwrite(&sum, sizeof(sum), 1, f) == 1;
+  if (fclose(f) != 0 || !ok) {
+    set_error(-17, "ostaple_net_weights_save: write to %s failed", path);
+    return -17;
+  }
+  return 0;
+}
+
+int ostaple_net_weights_load(const char* path, float* w) {
+  FILE* f = fopen(path, "rb");
+  if (!f) {
+    set_error(-17, "ostaple_net_weights_load: cannot open %s", path);
+    return -17;
+  }
+  NetFileHeader h;
+  const size_t nw = size_t(NET_LAYERS) * NET_K * NET_C;
+  std::vector<float> buf(nw);
+  uint64_t stored = 0;
+  const bool ok = fread(&h, sizeof(h), 1, f) == 1 && fread(buf.data(), sizeof(float), nw, f) == nw &&
+                  fread(&stored, sizeof(stored), 1, f) == 1;
+  fclose(f);
+  if (!ok) {
+    set_error(-18, "ostaple_net_weights_load: %s is truncated", path);
+    return -18;
+  }
+  if (memcmp(h.magic, kNetMagic, 8) != 0 || h.version != kNetVersion || h.layers != uint32_t(NET_LAYERS) ||
+      h.rows != uint32_t(NET_K) || h.cols != uint32_t(NET_C)) {
+    set_error(-18, "ostaple_net_weights_load: %s is not a version-%u weight file of shape %dx%dx%d", path,
+              kNetVersion, NET_LAYERS, NET_K, NET_C);
+    return -18;
+  }
+  uint64_t sum = fnv1a64(reinterpret_cast<const unsigned char*>(&h), sizeof(h));
+  sum = fnv1a64(reinterpret_cast<const unsigned char*>(buf.data()), nw * sizeof(float), sum);
+  if (sum != stored) {
+    set_error(-19, "ostaple_net_weights_load: checksum mismatch in %s", path);
+    return -19;
+  }
+  memcpy(w, buf.data(), nw * sizeof(float));
+  return 0;
+}
 
 int ostaple_net_init(unsigned seed, double scale) {
   if (!require_init("ostaple_net_init")) return -2;

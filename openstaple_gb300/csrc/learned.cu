@@ -481,3 +481,25 @@ void net_zero_dw(const NetBuffers& nb, cudaStream_t st) {
 }
 
 }  // namespace ost
+
+namespace ost {
+
+// Self-test of the bounded-wait path used by every tensor-core kernel: one
+// thread initialises an mbarrier for one arrival, arrives on it or not, and
+// waits with the same bounded poll as the MMA completion waits.  Without the
+// arrival the wait runs out after `polls` polls and the error word is set,
+// exactly as a lost MMA completion would; the kernel returns normally.
+__global__ void k_wait_selftest(int signal, long polls, int* err) {
+  __shared__ __align__(8) uint64_t mbar;
+  if (threadIdx.x != 0) return;
+  tc::mbar_init(&mbar, 1);
+  if (signal) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(tc::smem_u32(&mbar)) : "memory");
+  if (!tc::mbar_wait_bounded(&mbar, 0, polls)) atomicExch(err, 1);
+}
+
+void net_wait_selftest(const NetBuffers& nb, int signal, long polls, cudaStream_t st) {
+  k_wait_selftest<<<1, 32, 0, st>>>(signal, polls, nb.err);
+  OST_LAUNCH_CHECK();
+}
+
+}  // namespace ost

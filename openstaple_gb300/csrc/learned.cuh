@@ -53,5 +53,8 @@ void net_layer_backward(const NetBuffers& nb, int layer, const float2* u32, cons
 void net_adam_step(const NetBuffers& nb, float lr, float beta1, float beta2, float eps, int t, cudaStream_t st);
 void net_sync_weights(const NetBuffers& nb, cudaStream_t st);   // master FP32 -> BF16 MMA copy
 void net_zero_dw(const NetBuffers& nb, cudaStream_t st);
+// bounded mbarrier wait with (signal = 1) or without its arrival; a timeout
+// sets nb.err like a lost MMA completion
+void net_wait_selftest(const NetBuffers& nb, int signal, long polls, cudaStream_t st);
 
 }  // namespace ost

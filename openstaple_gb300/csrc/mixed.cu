@@ -307,6 +307,14 @@ MixedResult mixed_cg(const MixedBuffers& B, const MixedOptions& o, MixScal* sc, 
   OST_CUDA(cudaStreamSynchronize(cs));
   const double bn = g_host->bnorm2;
   const bool zero_guess = g_host->true_r2 == 0.0;
+  if (!std::isfinite(bn) || !std::isfinite(g_host->true_r2)) {
+    // a non-finite source or guess cannot converge: report failure at once
+    // instead of iterating on NaNs up to max_iter
+    OST_CUDA(cudaEventRecord(ev, cs));
+    OST_CUDA(cudaStreamWaitEvent(st, ev, 0));
+    OST_CUDA(cudaEventDestroy(ev));
+    return res;
+  }
   double fp32_target = o.safety * o.res;
   init.target2 = fp32_target * fp32_target * bn;
   init.bnorm2 = bn;

@@ -112,6 +112,9 @@ SIGNATURES = {
     "real_scal_prod_global": (_D, [_P, _P]),
     "l2norm2_global": (_D, [_P]),
     "ostaple_mdagm_df": (_I, [_P, _P, _D, _D, _P, _P]),
+    "ostaple_net_weights_save": (_I, [C.c_char_p, _P]),
+    "ostaple_net_weights_load": (_I, [C.c_char_p, _P]),
+    "ostaple_selftest_bounded_wait": (_I, [_I]),
     "ostaple_real_scal_prod_global_noalloc": (_D, [_P, _P]),
     "combine_in1xfactor_plus_in2": (None, [_P, _D, _P, _P]),
     "multiply_fermion_x_doublefactor": (None, [_P, _D]),
