@@ -40,19 +40,26 @@ OST_D HopCtx hop_ctx(const int fwd[4], const int bwd[4], int idx, int d, int p_o
   return h;
 }
 
-// h[a][c], a = 2*colour + (0 re, 1 im), for the 8 channels of activation act
-OST_D void transport8(const LinkView<float2>& u, const unsigned char* signs, long sh, const HopCtx& hc,
-                      const __nv_bfloat162* act, float h[6][NET_C]) {
+// h[a][c], a = 2*colour + (0 re, 1 im), for channels c0 .. c0+NCH-1 of
+// activation act
+template <int NCH>
+OST_D void transport_ch(const LinkView<float2>& u, const unsigned char* signs, long sh, const HopCtx& hc,
+                        const __nv_bfloat162* act, int c0, float h[6][NCH]) {
   float2 m[6];
   load_two_rows(u, hc.dir, hc.li, m);
   const unsigned char sb = __ldg(signs + long(hc.dir) * sh + hc.li);
   const unsigned mask = sb ? 0x80000000u : 0u;
+  float2 vin[NCH][3];
 #pragma unroll
-  for (int c = 0; c < NET_C; ++c) {
+  for (int c = 0; c < NCH; ++c)     // every load of the hop first
+#pragma unroll
+    for (int col = 0; col < 3; ++col) vin[c][col] = __bfloat1622float2(act[(long(c0 + c) * 3 + col) * sh + hc.j]);
+#pragma unroll
+  for (int c = 0; c < NCH; ++c) {
     float2 v[3], aux[3];
 #pragma unroll
     for (int col = 0; col < 3; ++col) {
-      float2 f = __bfloat1622float2(act[(long(c) * 3 + col) * sh + hc.j]);
+      float2 f = vin[c][col];
       f.x = flip_sign(f.x, mask);
       f.y = flip_sign(f.y, mask);
       v[col] = f;
@@ -65,6 +72,11 @@ OST_D void transport8(const LinkView<float2>& u, const unsigned char* signs, lon
   }
 }
 
+OST_D void transport8(const LinkView<float2>& u, const unsigned char* signs, long sh, const HopCtx& hc,
+                      const __nv_bfloat162* act, float h[6][NET_C]) {
+  transport_ch<NET_C>(u, signs, sh, hc, act, 0, h);
+}
+
 OST_D uint4 pack8_bf16(const float* v) {
   __nv_bfloat162 a = __floats2bfloat162_rn(v[0], v[1]), b = __floats2bfloat162_rn(v[2], v[3]);
   __nv_bfloat162 c = __floats2bfloat162_rn(v[4], v[5]), d = __floats2bfloat162_rn(v[6], v[7]);
@@ -74,13 +86,25 @@ OST_D uint4 pack8_bf16(const float* v) {
   return r;
 }
 
+OST_D uint2 pack4_bf16(const float* v) {
+  __nv_bfloat162 a = __floats2bfloat162_rn(v[0], v[1]), b = __floats2bfloat162_rn(v[2], v[3]);
+  uint2 r;
+  r.x = *reinterpret_cast<uint32_t*>(&a);
+  r.y = *reinterpret_cast<uint32_t*>(&b);
+  return r;
+}
+
 // ---- forward layer ----
-// dynamic shared memory: 6 A tiles [128 x 64] BF16 (16 KB each), B tile [16 x 64] BF16
+// dynamic shared memory: 6 A tiles [128 x 64] BF16 (16 KB each), B tile [16 x 64] BF16.
+// Two threads per site: thread half 0 transports channels 0-3, half 1
+// channels 4-7, so a tile of 128 sites runs 8 warps (two CTAs per SM).
 static constexpr int FWD_A_BYTES = NT * NET_K * 2;
 static constexpr int FWD_SMEM = 6 * FWD_A_BYTES + NET_N * NET_K * 2;
+static constexpr int FWD_THREADS = 2 * NT;
+static constexpr int FWD_HALF = NET_C / 2;
 
 template <int P_OUT, bool OUT_F32>
-__global__ void __launch_bounds__(NT, 1)
+__global__ void __launch_bounds__(FWD_THREADS, 2)
 k_net_fwd(Geom g, LinkView<float2> u, const unsigned char* __restrict__ signs, const __nv_bfloat162* __restrict__ act_in,
           const __nv_bfloat16* __restrict__ w, __nv_bfloat162* __restrict__ act_out, float2* __restrict__ out_f32,
           int* err) {
@@ -88,15 +112,17 @@ k_net_fwd(Geom g, LinkView<float2> u, const unsigned char* __restrict__ signs, c
   __shared__ uint64_t mbar;
   __shared__ uint32_t tslot;
   const int tid = threadIdx.x, warp = tid >> 5;
+  const int row = tid & (NT - 1);          // site of the tile = TMEM lane
+  const int half = tid / NT;               // channel half
   const long sh = g.sizeh;
-  const int idx = blockIdx.x * NT + tid;
+  const int idx = blockIdx.x * NT + row;
   const bool valid = idx < g.sizeh;
   unsigned char* Abase = smem;
   unsigned char* B = smem + 6 * FWD_A_BYTES;
   if (warp == 0) tc::tmem_alloc(&tslot, 128);
   if (tid == 0) tc::mbar_init(&mbar, 1);
   // weights as the B operand: B[n][k] = W[k][n]
-  for (int e = tid; e < NET_N * NET_K; e += NT) {
+  for (int e = tid; e < NET_N * NET_K; e += FWD_THREADS) {
     const int n = e / NET_K, k = e % NET_K;
     *reinterpret_cast<__nv_bfloat16*>(B + tc::kmajor_offset(n, k, NET_K)) = w[e];
   }
@@ -105,20 +131,21 @@ k_net_fwd(Geom g, LinkView<float2> u, const unsigned char* __restrict__ signs, c
     Site s = site_of(g, idx, P_OUT);
     neighbours(g, s, fwd, bwd);
   }
-#pragma unroll 1
+#pragma unroll 2
   for (int d = 0; d < 8; ++d) {
-    float h[6][NET_C];
+    float h[6][FWD_HALF];
     if (valid) {
-      transport8(u, signs, sh, hop_ctx(fwd, bwd, idx, d, P_OUT), act_in, h);
+      transport_ch<FWD_HALF>(u, signs, sh, hop_ctx(fwd, bwd, idx, d, P_OUT), act_in, half * FWD_HALF, h);
     } else {
 #pragma unroll
       for (int a = 0; a < 6; ++a)
 #pragma unroll
-        for (int c = 0; c < NET_C; ++c) h[a][c] = 0.f;
+        for (int c = 0; c < FWD_HALF; ++c) h[a][c] = 0.f;
     }
 #pragma unroll
     for (int a = 0; a < 6; ++a)
-      *reinterpret_cast<uint4*>(Abase + a * FWD_A_BYTES + tc::kmajor_offset(tid, d * NET_C, NET_K)) = pack8_bf16(h[a]);
+      *reinterpret_cast<uint2*>(Abase + a * FWD_A_BYTES + tc::kmajor_offset(row, d * NET_C + half * FWD_HALF, NET_K)) =
+          pack4_bf16(h[a]);
   }
   tc::fence_async_smem();
   tc::fence_before_sync();
@@ -138,19 +165,27 @@ k_net_fwd(Geom g, LinkView<float2> u, const unsigned char* __restrict__ signs, c
   const bool ok = tc::mbar_wait_bounded(&mbar, 0, WAIT_LIMIT);
   if (!ok && (tid & 31) == 0) atomicExch(err, 1);
   tc::fence_after_sync();
+  // a warp reads the TMEM lanes of its sub-partition (warp % 4): both
+  // halves see the same 32 sites and store their own output channels
   float o[6][NET_N];
 #pragma unroll
-  for (int a = 0; a < 6; ++a) tc::tmem_ld16(taddr + (uint32_t(warp * 32) << 16) + a * NET_N, o[a]);
+  for (int a = 0; a < 6; ++a) tc::tmem_ld16(taddr + (uint32_t((warp & 3) * 32) << 16) + a * NET_N, o[a]);
   if (valid && ok) {
     if (OUT_F32) {
+      if (half == 0) {
 #pragma unroll
-      for (int col = 0; col < 3; ++col) out_f32[col * sh + idx] = make_float2(o[2 * col][0], o[2 * col + 1][0]);
+        for (int col = 0; col < 3; ++col) out_f32[col * sh + idx] = make_float2(o[2 * col][0], o[2 * col + 1][0]);
+      }
     } else {
 #pragma unroll
-      for (int c = 0; c < NET_C; ++c)
+      for (int c = 0; c < FWD_HALF; ++c)
 #pragma unroll
-        for (int col = 0; col < 3; ++col)
-          act_out[(long(c) * 3 + col) * sh + idx] = __floats2bfloat162_rn(o[2 * col][c], o[2 * col + 1][c]);
+        for (int col = 0; col < 3; ++col) {
+          // compile-time register indices, selected by the half
+          const float re = half ? o[2 * col][FWD_HALF + c] : o[2 * col][c];
+          const float im = half ? o[2 * col + 1][FWD_HALF + c] : o[2 * col + 1][c];
+          act_out[(long(half * FWD_HALF + c) * 3 + col) * sh + idx] = __floats2bfloat162_rn(re, im);
+        }
     }
   }
   tc::fence_before_sync();
@@ -418,9 +453,9 @@ void net_layer_forward(const NetBuffers& nb, int layer, const float2* u32, const
   const __nv_bfloat16* w = nb.w_mma + size_t(layer) * NET_N * NET_K;
   const bool last = layer == NET_LAYERS - 1;
   __nv_bfloat162* out = last ? nullptr : act_of(nb, layer + 1);
-  if (p_out == 1 && !last) k_net_fwd<1, false><<<nb_, NT, FWD_SMEM, st>>>(g, u, signs, act_of(nb, layer), w, out, out_f32, nb.err);
-  else if (p_out == 0 && !last) k_net_fwd<0, false><<<nb_, NT, FWD_SMEM, st>>>(g, u, signs, act_of(nb, layer), w, out, out_f32, nb.err);
-  else k_net_fwd<0, true><<<nb_, NT, FWD_SMEM, st>>>(g, u, signs, act_of(nb, layer), w, out, out_f32, nb.err);
+  if (p_out == 1 && !last) k_net_fwd<1, false><<<nb_, FWD_THREADS, FWD_SMEM, st>>>(g, u, signs, act_of(nb, layer), w, out, out_f32, nb.err);
+  else if (p_out == 0 && !last) k_net_fwd<0, false><<<nb_, FWD_THREADS, FWD_SMEM, st>>>(g, u, signs, act_of(nb, layer), w, out, out_f32, nb.err);
+  else k_net_fwd<0, true><<<nb_, FWD_THREADS, FWD_SMEM, st>>>(g, u, signs, act_of(nb, layer), w, out, out_f32, nb.err);
   OST_LAUNCH_CHECK();
 }
 
