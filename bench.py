@@ -59,6 +59,10 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--skip-fp64", action="store_true", help="skip the plain FP64 CG arm (profiling runs)")
+    ap.add_argument("--solver", default="mixed", choices=["mixed", "learned"],
+                    help="learned: flexible CG preconditioned by the network, trained before the timed region "
+                         "on solver-produced pairs")
+    ap.add_argument("--train-epochs", type=int, default=150)
     ap.add_argument("--rhs", type=int, default=1,
                     help="right-hand sides per step; >1 solves them together with the batched solver")
     ap.add_argument("--delta", type=float, default=1e-4,
@@ -255,7 +259,31 @@ def main():
     for a in work:
         lat.release(a)
 
+    learned = None
+    if args.solver == "learned":
+        # training pairs (b_i, x_i) from the batched solver, then GPU training
+        from openstaple_gb300 import fields as F
+        tb = np.stack([F.gaussian_vec3(dims, args.seed + 17 * rank + 500 + k) for k in range(8)])
+        tx = lat.vec3(8)
+        lat.present(tb)
+        lat.present(tx)
+        t0 = time.perf_counter()
+        api.invert_mixed_batch(u, ph, args.mass, tx, tb, None, args.res, 100000, args.delta)
+        t1 = time.perf_counter()
+        api.net_init(11, 0.05)
+        hist = api.net_train(u, ph, args.mass, tb, tx, args.train_epochs, 3e-3)
+        t2 = time.perf_counter()
+        learned = {"pairs": 8, "pair_generation_s": t1 - t0, "epochs": args.train_epochs, "training_s": t2 - t1,
+                   "loss_first": float(hist[0]), "loss_last": float(hist[-1])}
+        lat.release(tb)
+        lat.release(tx)
+
     def solve():
+        if args.solver == "learned":
+            L.set_vec3_soa_to_zero(x.ctypes.data)
+            r = api.invert_learned(u, ph, args.mass, 0.0, x, b, args.res, 5000)
+            learned["used_fallback"] = r["used_fallback"]
+            return dict(status=r["status"], iters=r["iters"], true_res=r["true_res"], n_reliable=-1)
         if nrhs > 1:
             for k in range(nrhs):
                 L.set_vec3_soa_to_zero(xs[k].ctypes.data)
@@ -267,7 +295,7 @@ def main():
 
     # the same workload with 4 right-hand sides solved together (reported beside the headline)
     batched4 = None
-    if nrhs == 1 and not args.skip_fp64:
+    if nrhs == 1 and not args.skip_fp64 and args.solver == "mixed":
         from openstaple_gb300 import fields as F
         b4 = np.stack([b] + [F.gaussian_vec3(dims, args.seed + 17 * rank + 100 + k) for k in range(3)])
         x4 = lat.vec3(4)
@@ -336,7 +364,9 @@ def main():
             t0 = time.perf_counter()
             for a in (u, ph, be, xe):
                 lat.update_device(a)
-            if nrhs > 1:
+            if args.solver == "learned":
+                api.invert_learned(u, ph, args.mass, 0.0, xe, be, args.res, 5000)
+            elif nrhs > 1:
                 api.invert_mixed_batch(u, ph, args.mass, xe, be, None, args.res, 100000, args.delta)
             else:
                 api.invert_mixed(u, ph, args.mass, 0.0, xe, be, args.res, 100000, 0, args.delta)
@@ -360,9 +390,12 @@ def main():
             "data": "synthetic (seeded exp(i*0.3*H) links, Gaussian source)",
             "config": {"workload": f"MdagM solve {'x'.join(map(str, dims))} m={args.mass} to FP64 true residual "
                                    f"{args.res}",
-                       "solver": ("mixed-precision CG (FP32 iteration, double-float reliable updates, FP64 final "
+                       "solver": ("flexible CG preconditioned by the learned gauge-covariant network (tcgen05 BF16), "
+                                  "plain CG fallback" if args.solver == "learned" else
+                                  "mixed-precision CG (FP32 iteration, double-float reliable updates, FP64 final "
                                   "residual, CUDA-graph chunks)" if nrhs == 1 else
                                   f"batched mixed-precision CG, {nrhs} right-hand sides sharing each link load"),
+                       "learned": learned,
                        "rhs_per_step": nrhs,
                        "batched_4rhs": batched4,
                        "iterations": infos[-1]["iters"], "reliable_updates": infos[-1]["n_reliable"],

@@ -48,25 +48,33 @@ OST_D void transport_ch(const LinkView<float2>& u, const unsigned char* signs, l
   float2 m[6];
   load_two_rows(u, hc.dir, hc.li, m);
   const unsigned char sb = __ldg(signs + long(hc.dir) * sh + hc.li);
-  const unsigned mask = sb ? 0x80000000u : 0u;
   float2 vin[NCH][3];
 #pragma unroll
   for (int c = 0; c < NCH; ++c)     // every load of the hop first
 #pragma unroll
     for (int col = 0; col < 3; ++col) vin[c][col] = __bfloat1622float2(act[(long(c0 + c) * 3 + col) * sh + hc.j]);
+  // the staggered sign multiplies the whole matrix (third row rebuilt from the
+  // unsigned rows, then all nine entries flipped) instead of every channel
+  float2 r3[3] = {conj_cross(m[1], m[5], m[2], m[4]), conj_cross(m[2], m[3], m[0], m[5]),
+                  conj_cross(m[0], m[4], m[1], m[3])};
+  const unsigned mask = sb ? 0x80000000u : 0u;
+#pragma unroll
+  for (int e = 0; e < 6; ++e) { m[e].x = flip_sign(m[e].x, mask); m[e].y = flip_sign(m[e].y, mask); }
+#pragma unroll
+  for (int e = 0; e < 3; ++e) { r3[e].x = flip_sign(r3[e].x, mask); r3[e].y = flip_sign(r3[e].y, mask); }
 #pragma unroll
   for (int c = 0; c < NCH; ++c) {
-    float2 v[3], aux[3];
-#pragma unroll
-    for (int col = 0; col < 3; ++col) {
-      float2 f = vin[c][col];
-      f.x = flip_sign(f.x, mask);
-      f.y = flip_sign(f.y, mask);
-      v[col] = f;
-      aux[col] = make_float2(0.f, 0.f);
+    float2 aux[3] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+    const float2* v = vin[c];
+    if (hc.back) {   // U^+ v
+      cmacc(aux[0], m[0], v[0]); cmacc(aux[0], m[3], v[1]); cmacc(aux[0], r3[0], v[2]);
+      cmacc(aux[1], m[1], v[0]); cmacc(aux[1], m[4], v[1]); cmacc(aux[1], r3[1], v[2]);
+      cmacc(aux[2], m[2], v[0]); cmacc(aux[2], m[5], v[1]); cmacc(aux[2], r3[2], v[2]);
+    } else {         // U v
+      cmac(aux[0], m[0], v[0]); cmac(aux[0], m[1], v[1]); cmac(aux[0], m[2], v[2]);
+      cmac(aux[1], m[3], v[0]); cmac(aux[1], m[4], v[1]); cmac(aux[1], m[5], v[2]);
+      cmac(aux[2], r3[0], v[0]); cmac(aux[2], r3[1], v[1]); cmac(aux[2], r3[2], v[2]);
     }
-    if (hc.back) mac_Udag(aux, m, v);
-    else mac_U(aux, m, v);
 #pragma unroll
     for (int col = 0; col < 3; ++col) { h[2 * col][c] = aux[col].x; h[2 * col + 1][c] = aux[col].y; }
   }
@@ -131,7 +139,7 @@ k_net_fwd(Geom g, LinkView<float2> u, const unsigned char* __restrict__ signs, c
     Site s = site_of(g, idx, P_OUT);
     neighbours(g, s, fwd, bwd);
   }
-#pragma unroll 2
+#pragma unroll
   for (int d = 0; d < 8; ++d) {
     float h[6][FWD_HALF];
     if (valid) {
