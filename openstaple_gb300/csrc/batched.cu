@@ -117,16 +117,14 @@ OST_D void hop_multi(const Geom& g, const LinkView<float2>& u, const float2* in,
   }
 }
 
-// thread -> (site, lane, first system slot); slots beyond NS read a valid
-// system (slot 0) and discard the result.  Returns idx < sizeh.
+// thread -> (site, first system slot of its lane); slots beyond NS read a
+// valid system (slot 0) and discard the result.  Returns idx < sizeh.
 template <int NS>
-OST_D bool hop_thread(long sizeh, int& idx, int& lane, int& ls, int sys[HopLayout<NS>::SPL],
-                      bool valid[HopLayout<NS>::SPL]) {
+OST_D bool hop_thread(long sizeh, int& idx, int sys[HopLayout<NS>::SPL], bool valid[HopLayout<NS>::SPL]) {
   typedef HopLayout<NS> H;
   const long tid = long(blockIdx.x) * BT + threadIdx.x;
   idx = int(tid / H::LANES);
-  lane = int(tid % H::LANES);
-  ls = threadIdx.x / H::LANES;
+  const int lane = int(tid % H::LANES);
 #pragma unroll
   for (int j = 0; j < H::SPL; ++j) {
     const int k = lane * H::SPL + j;
@@ -144,9 +142,9 @@ k_b_doe(Geom g, LinkView<float2> u, const void* __restrict__ ph, const float2* _
         long vs, const BatchScal* sc) {
   typedef HopLayout<NS> H;
   if (!active_mask(sc)) return;
-  int idx, lane, ls, sys[H::SPL];
+  int idx, sys[H::SPL];
   bool valid[H::SPL];
-  const bool live = hop_thread<NS>(g.sizeh, idx, lane, ls, sys, valid);
+  const bool live = hop_thread<NS>(g.sizeh, idx, sys, valid);
   float2 aux[H::SPL][3];
   if (live) hop_multi<H::SPL, 1, PH>(g, u, p, vs, sys, ph, idx, aux);
   if (!live) return;
@@ -198,9 +196,9 @@ k_b_deo_dot(Geom g, LinkView<float2> u, const void* __restrict__ ph, const float
             const float2* __restrict__ p, float2* __restrict__ s, long vs, BatchScal* sc, ReduceWs ws) {
   typedef HopLayout<NS> H;
   if (!active_mask(sc)) return;
-  int idx, lane, ls, sys[H::SPL];
+  int idx, sys[H::SPL];
   bool valid[H::SPL];
-  const bool live = hop_thread<NS>(g.sizeh, idx, lane, ls, sys, valid);
+  const bool live = hop_thread<NS>(g.sizeh, idx, sys, valid);
   float v[H::SPL];
   float2 aux[H::SPL][3];
   if (live) hop_multi<H::SPL, 0, PH>(g, u, t, vs, sys, ph, idx, aux);
@@ -618,9 +616,9 @@ k_cgm_doe(Geom g, LinkView<float2> u, const void* __restrict__ ph, const float2*
           long vs, const CgmScal* sc) {
   typedef HopLayout<NR> H;
   if (!cgm_mask(sc)) return;
-  int idx, lane, ls, sys[H::SPL];
+  int idx, sys[H::SPL];
   bool valid[H::SPL];
-  const bool live = hop_thread<NR>(g.sizeh, idx, lane, ls, sys, valid);
+  const bool live = hop_thread<NR>(g.sizeh, idx, sys, valid);
   float2 aux[H::SPL][3];
   if (live) hop_multi<H::SPL, 1, PH>(g, u, p, vs, sys, ph, idx, aux);
   if (!live) return;
@@ -641,9 +639,9 @@ k_cgm_deo_dot(Geom g, LinkView<float2> u, const void* __restrict__ ph, const flo
               const float2* __restrict__ p, float2* __restrict__ s, long vs, CgmScal* sc, ReduceWs ws) {
   typedef HopLayout<NR> H;
   if (!cgm_mask(sc)) return;
-  int idx, lane, ls, sys[H::SPL];
+  int idx, sys[H::SPL];
   bool valid[H::SPL];
-  const bool live = hop_thread<NR>(g.sizeh, idx, lane, ls, sys, valid);
+  const bool live = hop_thread<NR>(g.sizeh, idx, sys, valid);
   float v[H::SPL];
   float2 aux[H::SPL][3];
   if (live) hop_multi<H::SPL, 0, PH>(g, u, t, vs, sys, ph, idx, aux);
