@@ -40,8 +40,10 @@ PROFILE_TRAFFIC = ROOT / "profiles" / "traffic.json"
 FALLBACK_HBM = 6800.0
 
 # algorithmic bytes per output site of one hop application
-# D_oe of the mixed solver per output site: links (2 rows FP32) + sign bytes + r and p_old in + p_new and t out
-BYTES_F32_SIGN = 8 * 12 * 4 + 8 * 1 + 2 * 3 * 8 + 2 * 3 * 8   # = 488
+# D_oe of the mixed solver per output site: links (2 rows FP32) + sign bytes + in + out
+BYTES_F32_SIGN = 8 * 12 * 4 + 8 * 1 + 3 * 8 + 3 * 8      # = 440
+# D_eo + M^+M epilogue + <p,s> per output site: links + sign bytes + t and p in + s out
+BYTES_F32_DEO = 8 * 12 * 4 + 8 * 1 + 2 * 3 * 8 + 3 * 8        # = 464
 BYTES_F64_ANGLE = 8 * 12 * 8 + 8 * 8 + 3 * 16 + 3 * 16   # links(2 rows) + angles + in + out = 928
 
 
@@ -332,17 +334,21 @@ def main():
     value = world * nrhs * 1e3 / ms
     ok = all(i["status"] == 1 and i["true_res"] <= args.res for i in infos)
 
-    # roofline of the dominant kernel (the FP32 hop of the mixed solver), timed alone
+    # roofline of the dominant kernel of the solve (the FP32 D_eo with the
+    # M^+M epilogue and <p, Ap>), and of the D_oe beside it, each timed alone
     hbm, peak_kind = peaks()
     kms = C.c_double(0)
-    L.ostaple_time_kernel(1, u.ctypes.data, ph.ctypes.data, 50, C.byref(kms))
-    achieved = BYTES_F32_SIGN * lat.sizeh / (kms.value * 1e-3) / 1e9
-    traffic = None
+    L.ostaple_time_kernel(2, u.ctypes.data, ph.ctypes.data, 50, C.byref(kms))
+    achieved = BYTES_F32_DEO * lat.sizeh / (kms.value * 1e-3) / 1e9
+    kdoe = C.c_double(0)
+    L.ostaple_time_kernel(1, u.ctypes.data, ph.ctypes.data, 50, C.byref(kdoe))
+    achieved_doe = BYTES_F32_SIGN * lat.sizeh / (kdoe.value * 1e-3) / 1e9
+    traffic, traffic_doe = None, None
     if PROFILE_TRAFFIC.exists():
         tr = json.loads(PROFILE_TRAFFIC.read_text())
-        key = f"dslash_f32_doe_{'x'.join(map(str, dims))}"
-        if key in tr:
-            traffic = tr[key]["bytes_per_launch"]
+        tag = 'x'.join(map(str, dims))
+        traffic = tr.get(f"dslash_f32_deo_dot_{tag}", {}).get("bytes_per_launch")
+        traffic_doe = tr.get(f"dslash_f32_doe_{tag}", {}).get("bytes_per_launch")
     k64 = C.c_double(0)
     L.ostaple_time_kernel(0, u.ctypes.data, ph.ctypes.data, 10, C.byref(k64))
     fp64_peak = C.c_double(0)
@@ -404,10 +410,13 @@ def main():
                        "speedup_vs_plain_fp64_cg": fp64["ms"] * nrhs / ms if fp64["ms"] else None,
                        "l2": "inputs larger than L2 (FP32 links 201 MB, FP64 links 604 MB > 129 MB)",
                        "parallelism": f"replicas x{world}"},
-            "roofline": {"kernel": "k_mx_doe (FP32 D_oe with the direction update, compact links + sign bytes)", "bound": "hbm",
-                         "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+            "roofline": {"kernel": "k_mx_deo_dot (FP32 D_eo + M^+M epilogue + <p,Ap>, compact links + sign bytes)",
+                         "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                          "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
-                         "traffic": traffic, "bytes_per_site": BYTES_F32_SIGN, "ms_per_launch": kms.value},
+                         "traffic": traffic, "bytes_per_site": BYTES_F32_DEO, "ms_per_launch": kms.value,
+                         "doe": {"kernel": "k_mx_doe (FP32 D_oe)", "achieved": achieved_doe,
+                                 "frac": achieved_doe / hbm, "traffic": traffic_doe, "bytes_per_site": BYTES_F32_SIGN,
+                                 "ms_per_launch": kdoe.value}},
             "fp64_dslash": {"ms_per_launch": k64.value,
                             "hbm_gbs": BYTES_F64_ANGLE * lat.sizeh / (k64.value * 1e-3) / 1e9,
                             "fp64_tflops_executed": dslash64_flops / (k64.value * 1e-3) / 1e12,

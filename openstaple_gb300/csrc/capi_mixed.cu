@@ -105,8 +105,7 @@ int inverter_mixed_precision(inverter_package ip, ferm_param* pars, vec3_soa* so
   B.s = ip.loc_s_f ? dev(reinterpret_cast<Zf*>(ip.loc_s_f), "loc_s_f") : ws_vec<Zf>(WS_VEC1, 2, 5);
   B.p = ip.loc_p_f ? dev(reinterpret_cast<Zf*>(ip.loc_p_f), "loc_p_f") : ws_vec<Zf>(WS_VEC1, 3, 5);
   B.xf = ip.out_f ? dev(reinterpret_cast<Zf*>(ip.out_f), "out_f") : ws_vec<Zf>(WS_VEC1, 4, 5);
-  B.p2 = ws_vec<Zf>(WS_PDIR, 0, 1);
-  if (!B.r64 || !B.t64 || !B.t64b || !B.r || !B.t || !B.s || !B.p || !B.p2 || !B.xf) return INVERTER_FAILURE;
+  if (!B.r64 || !B.t64 || !B.t64b || !B.r || !B.t || !B.s || !B.p || !B.xf) return INVERTER_FAILURE;
   PreparedF32 pf;
   if (!prepare_f32(B.u64, ip.u_f, static_cast<const double*>(B.ph64), &pf, st)) return INVERTER_FAILURE;
   B.u32 = pf.u32;
@@ -151,8 +150,7 @@ int ostaple_invert_mixed(const su3_soa* u, const double_soa* phases, double mass
   B.s = ws_vec<Zf>(WS_VEC1, 2, 5);
   B.p = ws_vec<Zf>(WS_VEC1, 3, 5);
   B.xf = ws_vec<Zf>(WS_VEC1, 4, 5);
-  B.p2 = ws_vec<Zf>(WS_PDIR, 0, 1);
-  if (!B.r64 || !B.t64 || !B.t64b || !B.r || !B.t || !B.s || !B.p || !B.p2 || !B.xf) return INVERTER_FAILURE;
+  if (!B.r64 || !B.t64 || !B.t64b || !B.r || !B.t || !B.s || !B.p || !B.xf) return INVERTER_FAILURE;
   PreparedF32 pf;
   if (!prepare_f32(B.u64, nullptr, static_cast<const double*>(B.ph64), &pf, st)) return INVERTER_FAILURE;
   B.u32 = pf.u32;
@@ -243,8 +241,6 @@ int ostaple_time_kernel(int which, const su3_soa* u, const double_soa* phases, i
   B.s = ws_vec<Zf>(WS_VEC1, 2, 5);
   B.p = ws_vec<Zf>(WS_VEC1, 3, 5);
   B.xf = ws_vec<Zf>(WS_VEC1, 4, 5);
-  B.p2 = ws_vec<Zf>(WS_PDIR, 0, 1);
-  if (!B.r || !B.t || !B.s || !B.p || !B.p2 || !B.xf) return -5;
   PreparedF32 pf;
   if (!prepare_f32(u64, nullptr, static_cast<const double*>(ph), &pf, st)) return -4;
   B.u32 = pf.u32;

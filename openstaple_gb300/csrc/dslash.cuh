@@ -126,41 +126,10 @@ struct PhaseView {
 };
 
 // The hop term at output index idx of parity P.
-// Input of a hop: a plain vec3 field ...
-template <typename C>
-struct VecIn {
-  const C* v;
-  OST_D void load(long sh, int j, C out[3]) const { load_vec(v, sh, j, out); }
-};
-// ... or the CG direction p = r + beta p_old formed while it is loaded
-// (same rounding as a separate p update: one FMA per component).
-struct AxpyIn {
-  const float2* r;
-  const float2* p;
-  float beta;
-  OST_D void load(long sh, int j, float2 out[3]) const {
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      const float2 rv = __ldg(r + c * sh + j), pv = __ldg(p + c * sh + j);
-      out[c] = make_float2(fmaf(beta, pv.x, rv.x), fmaf(beta, pv.y, rv.y));
-    }
-  }
-};
-
-template <typename T, int P, int PH, typename IN>
-OST_D void hop_in(const Geom& g, const LinkView<typename cplx_t<T>::type>& u, const IN& in, const void* phases,
-                  int idx, typename cplx_t<T>::type aux[3]);
-
 template <typename T, int P, int PH>
 OST_D void hop(const Geom& g, const LinkView<typename cplx_t<T>::type>& u,
                const typename cplx_t<T>::type* in, const void* phases, int idx,
                typename cplx_t<T>::type aux[3]) {
-  hop_in<T, P, PH>(g, u, VecIn<typename cplx_t<T>::type>{in}, phases, idx, aux);
-}
-
-template <typename T, int P, int PH, typename IN>
-OST_D void hop_in(const Geom& g, const LinkView<typename cplx_t<T>::type>& u, const IN& in, const void* phases,
-                  int idx, typename cplx_t<T>::type aux[3]) {
   typedef typename cplx_t<T>::type C;
   typedef typename SignMask<T>::type M;
   const long sh = g.sizeh;
@@ -177,7 +146,7 @@ OST_D void hop_in(const Geom& g, const LinkView<typename cplx_t<T>::type>& u, co
     const int j = bwd[mu];
     C m[6], v[3];
     load_two_rows(u, dir, j, m);
-    in.load(sh, j, v);
+    load_vec(in, sh, j, v);
     if (PH == PH_ANGLE) {
       T arg = __ldcs(static_cast<const T*>(phases) + long(dir) * sh + j);
       apply_angle_phase<T, true>(v, arg, SignMask<T>::neg);
@@ -199,7 +168,7 @@ OST_D void hop_in(const Geom& g, const LinkView<typename cplx_t<T>::type>& u, co
     const int j = fwd[mu];
     C m[6], v[3];
     load_two_rows(u, dir, idx, m);
-    in.load(sh, j, v);
+    load_vec(in, sh, j, v);
     if (PH == PH_ANGLE) {
       T arg = __ldcs(static_cast<const T*>(phases) + long(dir) * sh + idx);
       apply_angle_phase<T, false>(v, arg, M(0));

@@ -65,45 +65,26 @@ void phases_to_f32(const double* ph64, float* ph32, long sh, cudaStream_t st) {
 }
 
 // ---- FP32 iteration kernels ----
-// The direction update p = r + beta p_old is folded into the next D_oe: the
-// hop forms p at every neighbour from r and p_old as it loads them, and each
-// thread stores p at its own index into the other buffer of the pair (the
-// buffers alternate with the iteration count, so no kernel reads a buffer
-// that this one writes).  This saves a streaming pass over r and p per
-// iteration; the values are those of a separate update (one FMA each).
-OST_D float2* p_old_of(const MixScal* sc, float2* pa, float2* pb) { return (sc->iter & 1) ? pb : pa; }
-OST_D float2* p_cur_of(const MixScal* sc, float2* pa, float2* pb) { return (sc->iter & 1) ? pa : pb; }
-
-// p = r + beta p_old (stored) ; t = D_oe p
+// t = D_oe p
 template <int PH>
 __global__ void __launch_bounds__(MX_THREADS)
-k_mx_doe(Geom g, LinkView<float2> u, const void* __restrict__ ph, const float2* __restrict__ r, float2* pa,
-         float2* pb, float2* __restrict__ t, const MixScal* sc) {
+k_mx_doe(Geom g, LinkView<float2> u, const void* __restrict__ ph, const float2* __restrict__ p,
+         float2* __restrict__ t, const MixScal* sc) {
   if (halted(sc)) return;
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= g.sizeh) return;
-  const float2* p_old = p_old_of(sc, pa, pb);
-  float2* p_new = p_cur_of(sc, pa, pb);
-  const float beta = float(sc->beta);
-  const long sh = g.sizeh;
   float2 aux[3];
-  hop_in<float, 1, PH>(g, u, AxpyIn{r, p_old, beta}, ph, idx, aux);
+  hop<float, 1, PH>(g, u, p, ph, idx, aux);
 #pragma unroll
-  for (int c = 0; c < 3; ++c) {
-    const long q = c * sh + idx;
-    const float2 rv = r[q], pv = p_old[q];
-    p_new[q] = make_float2(fmaf(beta, pv.x, rv.x), fmaf(beta, pv.y, rv.y));
-    t[q] = make_float2(0.5f * aux[c].x, 0.5f * aux[c].y);
-  }
+  for (int c = 0; c < 3; ++c) t[c * long(g.sizeh) + idx] = make_float2(0.5f * aux[c].x, 0.5f * aux[c].y);
 }
 
 // s = m2 p - D_eo t ; pAp = Re<p, s> ; alpha = delta / pAp
 template <int PH>
 __global__ void __launch_bounds__(MX_THREADS)
 k_mx_deo_dot(Geom g, LinkView<float2> u, const void* __restrict__ ph, const float2* __restrict__ t,
-             float2* pa, float2* pb, float2* __restrict__ s, MixScal* sc, ReduceWs ws) {
+             const float2* __restrict__ p, float2* __restrict__ s, MixScal* sc, ReduceWs ws) {
   if (halted(sc)) return;
-  const float2* p = p_cur_of(sc, pa, pb);
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
   float v[1] = {0.0f};
   if (idx < g.sizeh) {
@@ -128,10 +109,9 @@ k_mx_deo_dot(Geom g, LinkView<float2> u, const void* __restrict__ ph, const floa
 
 // x_f += alpha p ; unless a reliable update is due: r -= alpha s, lambda = |r|^2,
 // beta = lambda / delta, delta = lambda.
-__global__ void k_mx_update(float4* __restrict__ xf, float4* __restrict__ r, float2* pa, float2* pb,
+__global__ void k_mx_update(float4* __restrict__ xf, float4* __restrict__ r, const float4* __restrict__ p,
                             const float4* __restrict__ s, long n4, MixScal* sc, ReduceWs ws) {
   if (halted(sc)) return;
-  const float4* __restrict__ p = reinterpret_cast<const float4*>(p_cur_of(sc, pa, pb));
   const double delta = sc->delta;
   const double lm = sc->last_max > delta ? sc->last_max : delta;
   const bool rel = sc->every > 0 ? ((sc->iter + 1) % sc->every == 0) : (delta < sc->frac * lm);
@@ -174,6 +154,21 @@ __global__ void k_mx_update(float4* __restrict__ xf, float4* __restrict__ r, flo
       sc->delta = tot[0];
       if (tot[0] <= sc->target2 || sc->iter >= sc->max_iter) sc->done = 1;
     }
+  }
+}
+
+// p = r + beta p
+__global__ void k_mx_pupdate(float4* __restrict__ p, const float4* __restrict__ r, long n4, const MixScal* sc,
+                             int guarded) {
+  if (guarded && halted(sc)) return;
+  const float b = float(sc->beta);
+  const long stride = long(gridDim.x) * blockDim.x;
+  for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n4; i += 2 * stride) {
+    const long j = i + stride;
+    float4 pv = p[i], rv = r[i], pw, rw;
+    if (j < n4) { pw = p[j]; rw = r[j]; }
+    p[i] = make_float4(fmaf(b, pv.x, rv.x), fmaf(b, pv.y, rv.y), fmaf(b, pv.z, rv.z), fmaf(b, pv.w, rv.w));
+    if (j < n4) p[j] = make_float4(fmaf(b, pw.x, rw.x), fmaf(b, pw.y, rw.y), fmaf(b, pw.z, rw.z), fmaf(b, pw.w, rw.w));
   }
 }
 
@@ -239,7 +234,7 @@ MixScal* g_host = nullptr;
 
 bool same_key(const MixedBuffers& a, const MixedBuffers& b) {
   return a.u32 == b.u32 && a.ph32 == b.ph32 && a.ph32_mode == b.ph32_mode && a.u32_compact == b.u32_compact &&
-         a.r == b.r && a.p == b.p && a.p2 == b.p2 && a.s == b.s && a.xf == b.xf && a.t == b.t;
+         a.r == b.r && a.p == b.p && a.s == b.s && a.xf == b.xf && a.t == b.t;
 }
 
 void fp64_mdagm(const MixedBuffers& B, double2* out, const double2* in, double2* tmp, double m2, cudaStream_t st) {
@@ -264,16 +259,19 @@ void enqueue_iteration(const MixedBuffers& B, MixScal* sc, cudaStream_t st) {
   int gd = nb;
   ReduceWs wsd = reduce_ws(1, gd > gr ? gd : gr);
   if (B.ph32_mode == PH_SIGN8) {
-    k_mx_doe<PH_SIGN8><<<nb, MX_THREADS, 0, st>>>(g, u, B.ph32, B.r, B.p, B.p2, B.t, sc);
-    k_mx_deo_dot<PH_SIGN8><<<nb, MX_THREADS, 0, st>>>(g, u, B.ph32, B.t, B.p, B.p2, B.s, sc, wsd);
+    k_mx_doe<PH_SIGN8><<<nb, MX_THREADS, 0, st>>>(g, u, B.ph32, B.p, B.t, sc);
+    k_mx_deo_dot<PH_SIGN8><<<nb, MX_THREADS, 0, st>>>(g, u, B.ph32, B.t, B.p, B.s, sc, wsd);
   } else {
-    k_mx_doe<PH_ANGLE><<<nb, MX_THREADS, 0, st>>>(g, u, B.ph32, B.r, B.p, B.p2, B.t, sc);
-    k_mx_deo_dot<PH_ANGLE><<<nb, MX_THREADS, 0, st>>>(g, u, B.ph32, B.t, B.p, B.p2, B.s, sc, wsd);
+    k_mx_doe<PH_ANGLE><<<nb, MX_THREADS, 0, st>>>(g, u, B.ph32, B.p, B.t, sc);
+    k_mx_deo_dot<PH_ANGLE><<<nb, MX_THREADS, 0, st>>>(g, u, B.ph32, B.t, B.p, B.s, sc, wsd);
   }
   g_kernel_launches += 2;
-  k_mx_update<<<gr, RED_THREADS, 0, st>>>(reinterpret_cast<float4*>(B.xf), reinterpret_cast<float4*>(B.r), B.p, B.p2,
+  k_mx_update<<<gr, RED_THREADS, 0, st>>>(reinterpret_cast<float4*>(B.xf), reinterpret_cast<float4*>(B.r),
+                                          reinterpret_cast<const float4*>(B.p),
                                           reinterpret_cast<const float4*>(B.s), n4, sc, wsd);
-  g_kernel_launches += 1;
+  k_mx_pupdate<<<gr, RED_THREADS, 0, st>>>(reinterpret_cast<float4*>(B.p), reinterpret_cast<const float4*>(B.r),
+                                           n4, sc, 1);
+  g_kernel_launches += 2;
 }
 
 }  // namespace
@@ -359,7 +357,7 @@ MixedResult mixed_cg(const MixedBuffers& B, const MixedOptions& o, MixScal* sc, 
   for (int guard = 0; guard < 1000000; ++guard) {
     if (error_code()) break;
     OST_CUDA(cudaGraphLaunch(g_cache.exec, cs));
-    g_kernel_launches += 3ull * o.chunk;
+    g_kernel_launches += 4ull * o.chunk;
     OST_CUDA(cudaMemcpyAsync(g_host, sc, sizeof(MixScal), cudaMemcpyDeviceToHost, cs));
     OST_CUDA(cudaStreamSynchronize(cs));
     const MixScal h = *g_host;
@@ -373,7 +371,10 @@ MixedResult mixed_cg(const MixedBuffers& B, const MixedOptions& o, MixScal* sc, 
       int gr = reduce_grid(n);
       k_mx_residual<<<gr, RED_THREADS, 0, cs>>>(B.b, B.t64, B.r64, B.r, B.p, n, sc, reduce_ws(2, gr), 1);
       OST_LAUNCH_CHECK();
-      continue;   // the next D_oe forms p = r + beta p with the new beta
+      k_mx_pupdate<<<reduce_grid(n4), RED_THREADS, 0, cs>>>(reinterpret_cast<float4*>(B.p),
+                                                            reinterpret_cast<const float4*>(B.r), n4, sc, 0);
+      OST_LAUNCH_CHECK();
+      continue;
     }
     if (h.done) {
       // fold the FP32 correction in and measure the FP64 true residual
@@ -399,6 +400,9 @@ MixedResult mixed_cg(const MixedBuffers& B, const MixedOptions& o, MixScal* sc, 
       upd.target2 = fp32_target * fp32_target * bn;
       upd.done = (f.lambda <= upd.target2) ? 1 : 0;
       OST_CUDA(cudaMemcpyAsync(sc, &upd, sizeof(MixScal), cudaMemcpyHostToDevice, cs));
+      k_mx_pupdate<<<reduce_grid(n4), RED_THREADS, 0, cs>>>(reinterpret_cast<float4*>(B.p),
+                                                            reinterpret_cast<const float4*>(B.r), n4, sc, 0);
+      OST_LAUNCH_CHECK();
       continue;
     }
   }
@@ -429,12 +433,12 @@ double time_mixed_kernel(const MixedBuffers& B, MixScal* sc, int which, int reps
     cudaEventRecord(e0, st);
     for (int k = 0; k < reps; ++k) {
       if (which == 1) {
-        if (B.ph32_mode == PH_SIGN8) k_mx_doe<PH_SIGN8><<<nb, MX_THREADS, 0, st>>>(g, u, B.ph32, B.r, B.p, B.p2, B.t, sc);
-        else k_mx_doe<PH_ANGLE><<<nb, MX_THREADS, 0, st>>>(g, u, B.ph32, B.r, B.p, B.p2, B.t, sc);
+        if (B.ph32_mode == PH_SIGN8) k_mx_doe<PH_SIGN8><<<nb, MX_THREADS, 0, st>>>(g, u, B.ph32, B.p, B.t, sc);
+        else k_mx_doe<PH_ANGLE><<<nb, MX_THREADS, 0, st>>>(g, u, B.ph32, B.p, B.t, sc);
       } else {
         if (B.ph32_mode == PH_SIGN8)
-          k_mx_deo_dot<PH_SIGN8><<<nb, MX_THREADS, 0, st>>>(g, u, B.ph32, B.t, B.p, B.p2, B.s, sc, ws);
-        else k_mx_deo_dot<PH_ANGLE><<<nb, MX_THREADS, 0, st>>>(g, u, B.ph32, B.t, B.p, B.p2, B.s, sc, ws);
+          k_mx_deo_dot<PH_SIGN8><<<nb, MX_THREADS, 0, st>>>(g, u, B.ph32, B.t, B.p, B.s, sc, ws);
+        else k_mx_deo_dot<PH_ANGLE><<<nb, MX_THREADS, 0, st>>>(g, u, B.ph32, B.t, B.p, B.s, sc, ws);
       }
       OST_LAUNCH_CHECK();
     }

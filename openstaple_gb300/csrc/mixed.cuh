@@ -60,8 +60,7 @@ struct MixedBuffers {
   double2* t64;            // FP64 work
   double2* t64b;           // FP64 work (odd-parity temporary)
   float2* r;               // FP32 work
-  float2* p;               // CG direction, two buffers used alternately
-  float2* p2;
+  float2* p;
   float2* s;
   float2* xf;
   float2* t;               // odd-parity temporary

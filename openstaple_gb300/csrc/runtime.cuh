@@ -78,7 +78,6 @@ enum WorkspaceSlot {
   WS_BATCH64,
   WS_LINKS_LO,     // lo parts of the double-float links
   WS_DF,           // double-float M^+M work fields
-  WS_PDIR,         // second CG direction buffer of the mixed solver
   WS_NSLOTS
 };
 
