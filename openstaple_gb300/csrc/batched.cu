@@ -502,8 +502,10 @@ BatchResult batched_mixed_cg(const BatchBuffers& B, const double* m2, double res
   OST_CUDA(cudaMemcpyAsync(sc, &init, sizeof(BatchScal), cudaMemcpyHostToDevice, cs));
   blas_zero<float>(B.xf, NSY * n, cs);
   for (int k = 0; k < NSY; ++k) {
-    // r0 = b - A x0; a zero guess needs no operator application
+    // r0 = b - A x0; a zero guess needs no operator application, any other
+    // guess takes the double-float operator (the closing residual is FP64)
     if (zero_guess[k]) OST_CUDA(cudaMemsetAsync(B.t64, 0, n * sizeof(double2), cs));
+    else if (B.use_df) df_mdagm(B.df, B.dfw, B.t64, B.x + k * n, m2[k], cs);
     else fp64_mdagm(B, B.t64, B.x + k * n, m2[k], cs);
     const int gr = reduce_grid(n);
     k_b_residual<<<gr, RED_THREADS, 0, cs>>>(B.b + k * n, B.t64, B.r64, B.r + k * n, B.p + k * n, n, sc, k,

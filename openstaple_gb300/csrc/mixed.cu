@@ -320,6 +320,7 @@ MixedResult mixed_cg(const MixedBuffers& B, const MixedOptions& o, MixScal* sc, 
   blas_zero<float>(B.xf, n, cs);
   // r0 = b - A x0; a zero guess (the usual start) needs no operator application
   if (zero_guess) OST_CUDA(cudaMemsetAsync(B.t64, 0, n * sizeof(double2), cs));
+  else if (B.use_df) df_mdagm(B.df, B.dfw, B.t64, B.x, o.mass2, cs);   // the closing residual is FP64
   else fp64_mdagm(B, B.t64, B.x, B.t64b, o.mass2, cs);
   {
     int gr = reduce_grid(n);
