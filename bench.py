@@ -425,6 +425,7 @@ def main():
             "e2e": e2e,
             "gpu_launches": int(launches),
             "clocks": clk.summary(),
+            "autotune": api.autotune_report().splitlines(),
         }
         print(json.dumps(line))
     lat.close()

@@ -179,6 +179,20 @@ int ostaple_time_kernel(int which, const su3_soa *u, const double_soa *phases, i
  * counterpart. */
 int ostaple_probe_fma_tflops(int fp64, double *tflops);
 
+/* Launch-shape autotuner of the FP32 D_oe hops (the mixed solver's block
+ * size, the batched and multi-shift solvers' systems per thread).  Only
+ * shapes that leave every result bit unchanged are tuned; each (kernel,
+ * lattice) is timed once per process, before the solver captures its CUDA
+ * graph.  enable = 0 keeps the default shapes (so does OSTAPLE_AUTOTUNE=0 in
+ * the environment); enable = 2 + c forces candidate c of every tuned launch
+ * (c past a kernel's candidate list means its default), which tests use to
+ * check that each shape gives the same bits.  The report writes one line per tuned key (chosen
+ * candidate and each candidate's microseconds) into buf (NUL-terminated,
+ * truncated to len) and returns the full length.  No reference counterpart
+ * (the reference's launch shapes are fixed at compile time). */
+int ostaple_autotune(int enable);
+int ostaple_autotune_report(char *buf, int len);
+
 /* ---- staggered Dirac operator (fermion_matrix.h:20-39) ----------------- */
 /* out(even) = 1/2 sum_mu [ e^{i th} U_mu(x) in(x+mu) - e^{-i th} U_mu(x-mu)^+ in(x-mu) ] */
 void acc_Deo(const su3_soa *u, vec3_soa *out, const vec3_soa *in, const double_soa *backfield);

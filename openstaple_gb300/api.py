@@ -356,3 +356,17 @@ def invert_learned(u, phases, mass: float, shift: float, solution, inp, res: flo
                                       C.byref(it), C.byref(tr), C.byref(fb))
     check(0, "ostaple_invert_learned")
     return dict(status=st, iters=it.value, true_res=tr.value, used_fallback=fb.value)
+
+
+def autotune(enable: bool) -> None:
+    """Switch the launch-shape autotuner of the FP32 D_oe hops on or off."""
+    lib().ostaple_autotune(1 if enable else 0)
+
+
+def autotune_report() -> str:
+    """One line per tuned (kernel, lattice, variant): the chosen candidate and
+    each candidate's microseconds per launch."""
+    n = lib().ostaple_autotune_report(None, 0)
+    buf = C.create_string_buffer(n + 1)
+    lib().ostaple_autotune_report(buf, n + 1)
+    return buf.value.decode()

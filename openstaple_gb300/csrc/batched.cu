@@ -8,6 +8,7 @@
 // are captured as CUDA graphs and polled once per chunk.
 #include <cmath>
 #include <cstring>
+#include "autotune.cuh"
 #include "batched.cuh"
 #include "dslash.cuh"
 #include "kernels.cuh"
@@ -25,17 +26,17 @@ static constexpr int BT = 128;
 // link is fetched from memory once per batch.  The link loads, the staggered
 // sign and the rebuilt third row are shared by SPL systems per thread, while
 // the register footprint stays close to a single-system hop's.
-template <int NS>
+template <int NS, int SPL_ = 0>
 struct HopLayout {
-  static constexpr int SPL = NS <= 1 ? 1 : NS <= 4 ? 2 : 4;
+  static constexpr int SPL = SPL_ > 0 ? SPL_ : (NS <= 1 ? 1 : NS <= 4 ? 2 : 4);
   static constexpr int NL = (NS + SPL - 1) / SPL;
   static constexpr int LANES = NL <= 1 ? 1 : NL <= 2 ? 2 : NL <= 4 ? 4 : 8;
   static constexpr int SLOTS = LANES * SPL;   // per-site system slots, >= NS
 };
 
-template <int NS>
+template <int NS, int SPL_ = 0>
 inline int hop_blocks(long sizeh) {
-  return int((sizeh * HopLayout<NS>::LANES + BT - 1) / BT);
+  return int((sizeh * HopLayout<NS, SPL_>::LANES + BT - 1) / BT);
 }
 
 OST_D bool batch_active(const BatchScal* sc, int k) {
@@ -119,9 +120,9 @@ OST_D void hop_multi(const Geom& g, const LinkView<float2>& u, const float2* in,
 
 // thread -> (site, first system slot of its lane); slots beyond NS read a
 // valid system (slot 0) and discard the result.  Returns idx < sizeh.
-template <int NS>
-OST_D bool hop_thread(long sizeh, int& idx, int sys[HopLayout<NS>::SPL], bool valid[HopLayout<NS>::SPL]) {
-  typedef HopLayout<NS> H;
+template <int NS, int SPL_ = 0>
+OST_D bool hop_thread(long sizeh, int& idx, int sys[HopLayout<NS, SPL_>::SPL], bool valid[HopLayout<NS, SPL_>::SPL]) {
+  typedef HopLayout<NS, SPL_> H;
   const long tid = long(blockIdx.x) * BT + threadIdx.x;
   idx = int(tid / H::LANES);
   const int lane = int(tid % H::LANES);
@@ -136,15 +137,15 @@ OST_D bool hop_thread(long sizeh, int& idx, int sys[HopLayout<NS>::SPL], bool va
 
 // t_k = D_oe p_k (every system of the batch; converged ones are recomputed
 // harmlessly since t is a temporary)
-template <int NS, int PH>
+template <int NS, int SPL_, int PH>
 __global__ void __launch_bounds__(BT)
 k_b_doe(Geom g, LinkView<float2> u, const void* __restrict__ ph, const float2* __restrict__ p, float2* __restrict__ t,
         long vs, const BatchScal* sc) {
-  typedef HopLayout<NS> H;
+  typedef HopLayout<NS, SPL_> H;
   if (!active_mask(sc)) return;
   int idx, sys[H::SPL];
   bool valid[H::SPL];
-  const bool live = hop_thread<NS>(g.sizeh, idx, sys, valid);
+  const bool live = hop_thread<NS, SPL_>(g.sizeh, idx, sys, valid);
   float2 aux[H::SPL][3];
   if (live) hop_multi<H::SPL, 1, PH>(g, u, p, vs, sys, ph, idx, aux);
   if (!live) return;
@@ -373,6 +374,30 @@ __global__ void k_b_residual(const double2* __restrict__ b, const double2* __res
   }
 }
 
+// Launches of the D_oe hops with a given number of systems per thread
+// (0 = the default layout); the autotuner picks among them (no reduction,
+// so the results are the same for every choice).
+static const int kSplCand[4] = {0, 1, 2, 4};
+
+template <int NS, int SPL_>
+void launch_b_doe_spl(const BatchBuffers& B, BatchScal* sc, cudaStream_t st) {
+  const Geom& g = rt().g;
+  LinkView<float2> u{B.u32, g.sizeh, 6};
+  const long n = 3L * g.sizeh;
+  const int nb = hop_blocks<NS, SPL_>(g.sizeh);
+  if (B.ph32_mode == PH_SIGN8) k_b_doe<NS, SPL_, PH_SIGN8><<<nb, BT, 0, st>>>(g, u, B.ph32, B.p, B.t, n, sc);
+  else k_b_doe<NS, SPL_, PH_ANGLE><<<nb, BT, 0, st>>>(g, u, B.ph32, B.p, B.t, n, sc);
+  OST_LAUNCH_CHECK();
+}
+
+template <int NS>
+void launch_b_doe(int spl, const BatchBuffers& B, BatchScal* sc, cudaStream_t st) {
+  if (spl == 1) launch_b_doe_spl<NS, 1>(B, sc, st);
+  else if (spl == 2 && NS >= 2) launch_b_doe_spl<NS, 2>(B, sc, st);
+  else if (spl == 4 && NS >= 3) launch_b_doe_spl<NS, 4>(B, sc, st);
+  else launch_b_doe_spl<NS, 0>(B, sc, st);
+}
+
 // ---- host engine ----
 namespace {
 
@@ -382,6 +407,7 @@ struct BGraph {
   BatchScal* sc = nullptr;
   int chunk = 0;
   unsigned long long epoch = 0;
+  int doe_pick = -1;
 };
 BGraph g_bgraph;
 cudaStream_t g_bcap = nullptr;
@@ -406,13 +432,10 @@ void enqueue_batch_iteration(const BatchBuffers& B, BatchScal* sc, cudaStream_t 
   // one workspace for both reductions: hop (SLOTS x nb partials) and
   // segments (NS x bps partials)
   ReduceWs wh = reduce_ws(HopLayout<NS>::SLOTS, nb > NS * bps ? nb : NS * bps);
-  if (B.ph32_mode == PH_SIGN8) {
-    k_b_doe<NS, PH_SIGN8><<<nb, BT, 0, st>>>(g, u, B.ph32, B.p, B.t, n, sc);
-    k_b_deo_dot<NS, PH_SIGN8><<<nb, BT, 0, st>>>(g, u, B.ph32, B.t, B.p, B.s, n, sc, wh);
-  } else {
-    k_b_doe<NS, PH_ANGLE><<<nb, BT, 0, st>>>(g, u, B.ph32, B.p, B.t, n, sc);
-    k_b_deo_dot<NS, PH_ANGLE><<<nb, BT, 0, st>>>(g, u, B.ph32, B.t, B.p, B.s, n, sc, wh);
-  }
+  const int pick = autotune_cached(TUNE_B_DOE, g.sizeh, NS * 2 + (B.ph32_mode == PH_SIGN8));
+  launch_b_doe<NS>(kSplCand[pick > 0 && pick < 4 ? pick : 0], B, sc, st);
+  if (B.ph32_mode == PH_SIGN8) k_b_deo_dot<NS, PH_SIGN8><<<nb, BT, 0, st>>>(g, u, B.ph32, B.t, B.p, B.s, n, sc, wh);
+  else k_b_deo_dot<NS, PH_ANGLE><<<nb, BT, 0, st>>>(g, u, B.ph32, B.t, B.p, B.s, n, sc, wh);
   k_b_update<NS><<<NS * bps, RED_THREADS, 0, st>>>(reinterpret_cast<float4*>(B.xf), reinterpret_cast<float4*>(B.r),
                                                     reinterpret_cast<const float4*>(B.p),
                                                     reinterpret_cast<const float4*>(B.s), n4, n4, bps, sc, wh);
@@ -429,6 +452,33 @@ inline size_t batch_reduce_partials(long sizeh) {
   const long red = long(BATCH_MAX) * reduce_grid(3L * sizeh);
   long m = hop > seg ? hop : seg;
   return size_t(m > red ? m : red);
+}
+
+template <int NS>
+int tune_b_doe(const BatchBuffers& B, cudaStream_t st) {
+  const int variant = NS * 2 + (B.ph32_mode == PH_SIGN8);
+  const int cached = autotune_cached(TUNE_B_DOE, rt().g.sizeh, variant);
+  if (cached >= 0 || !autotune_enabled()) return cached > 0 ? cached : 0;
+  BatchScal h;
+  memset(&h, 0, sizeof(h));
+  h.nsys = NS;
+  BatchScal* sc = static_cast<BatchScal*>(autotune_scalars(&h, sizeof(h), st));
+  if (!sc) return 0;
+  return autotune_pick(TUNE_B_DOE, rt().g.sizeh, variant, 4,
+                       [&](int c) { launch_b_doe<NS>(kSplCand[c], B, sc, st); }, st);
+}
+
+int tune_batch(const BatchBuffers& B, cudaStream_t st) {
+  switch (B.nsys) {
+    case 1: return tune_b_doe<1>(B, st);
+    case 2: return tune_b_doe<2>(B, st);
+    case 3: return tune_b_doe<3>(B, st);
+    case 4: return tune_b_doe<4>(B, st);
+    case 5: return tune_b_doe<5>(B, st);
+    case 6: return tune_b_doe<6>(B, st);
+    case 7: return tune_b_doe<7>(B, st);
+    default: return tune_b_doe<8>(B, st);
+  }
 }
 
 void enqueue_chunk(const BatchBuffers& B, BatchScal* sc, int chunk, cudaStream_t st) {
@@ -521,7 +571,10 @@ BatchResult batched_mixed_cg(const BatchBuffers& B, const double* m2, double res
     finished[k] = true;
   }
   const int chunk = 8;
+  // launch shape of the D_oe (numerics-invariant), chosen before the capture
+  const int doe_pick = tune_batch(B, cs);
   if (!g_bgraph.exec || g_bgraph.sc != sc || g_bgraph.chunk != chunk || g_bgraph.key.nsys != B.nsys ||
+      g_bgraph.doe_pick != doe_pick ||
       g_bgraph.key.p != B.p || g_bgraph.key.r != B.r || g_bgraph.key.s != B.s || g_bgraph.key.t != B.t ||
       g_bgraph.key.xf != B.xf || g_bgraph.key.u32 != B.u32 || g_bgraph.key.ph32 != B.ph32 ||
       g_bgraph.key.ph32_mode != B.ph32_mode || g_bgraph.epoch != runtime_epoch()) {
@@ -536,6 +589,7 @@ BatchResult batched_mixed_cg(const BatchBuffers& B, const double* m2, double res
     g_bgraph.sc = sc;
     g_bgraph.chunk = chunk;
     g_bgraph.epoch = runtime_epoch();
+    g_bgraph.doe_pick = doe_pick;
   }
   for (int guard = 0; guard < 1000000; ++guard) {
     if (error_code()) break;
@@ -612,15 +666,15 @@ OST_D unsigned cgm_mask(const CgmScal* sc) {
 
 OST_D bool cgm_active(const CgmScal* sc, int r) { return !(*(volatile const int*)&sc->done[r]); }
 
-template <int NR, int PH>
+template <int NR, int SPL_, int PH>
 __global__ void __launch_bounds__(BT)
 k_cgm_doe(Geom g, LinkView<float2> u, const void* __restrict__ ph, const float2* __restrict__ p, float2* __restrict__ t,
           long vs, const CgmScal* sc) {
-  typedef HopLayout<NR> H;
+  typedef HopLayout<NR, SPL_> H;
   if (!cgm_mask(sc)) return;
   int idx, sys[H::SPL];
   bool valid[H::SPL];
-  const bool live = hop_thread<NR>(g.sizeh, idx, sys, valid);
+  const bool live = hop_thread<NR, SPL_>(g.sizeh, idx, sys, valid);
   float2 aux[H::SPL][3];
   if (live) hop_multi<H::SPL, 1, PH>(g, u, p, vs, sys, ph, idx, aux);
   if (!live) return;
@@ -631,6 +685,38 @@ k_cgm_doe(Geom g, LinkView<float2> u, const void* __restrict__ ph, const float2*
     for (int c = 0; c < 3; ++c)
       t[sys[j] * vs + c * long(g.sizeh) + idx] = make_float2(0.5f * aux[j][c].x, 0.5f * aux[j][c].y);
   }
+}
+
+template <int NR, int SPL_>
+void launch_cgm_doe_spl(const CgmBatchBuffers& B, const CgmScal* sc, cudaStream_t st) {
+  const Geom& g = rt().g;
+  LinkView<float2> u{B.u32, g.sizeh, 6};
+  const long n = 3L * g.sizeh;
+  const int nb = hop_blocks<NR, SPL_>(g.sizeh);
+  if (B.ph32_mode == PH_SIGN8) k_cgm_doe<NR, SPL_, PH_SIGN8><<<nb, BT, 0, st>>>(g, u, B.ph32, B.p, B.t, n, sc);
+  else k_cgm_doe<NR, SPL_, PH_ANGLE><<<nb, BT, 0, st>>>(g, u, B.ph32, B.p, B.t, n, sc);
+  OST_LAUNCH_CHECK();
+}
+
+template <int NR>
+void launch_cgm_doe(int spl, const CgmBatchBuffers& B, const CgmScal* sc, cudaStream_t st) {
+  if (spl == 1) launch_cgm_doe_spl<NR, 1>(B, sc, st);
+  else if (spl == 2 && NR >= 2) launch_cgm_doe_spl<NR, 2>(B, sc, st);
+  else if (spl == 4 && NR >= 3) launch_cgm_doe_spl<NR, 4>(B, sc, st);
+  else launch_cgm_doe_spl<NR, 0>(B, sc, st);
+}
+
+template <int NR>
+void tune_cgm_doe(const CgmBatchBuffers& B, cudaStream_t st) {
+  const int variant = NR * 2 + (B.ph32_mode == PH_SIGN8);
+  if (autotune_cached(TUNE_CGM_DOE, rt().g.sizeh, variant) >= 0 || !autotune_enabled()) return;
+  CgmScal h;
+  memset(&h, 0, sizeof(h));
+  h.nrhs = NR;
+  const CgmScal* sc = static_cast<const CgmScal*>(autotune_scalars(&h, sizeof(h), st));
+  if (!sc) return;
+  autotune_pick(TUNE_CGM_DOE, rt().g.sizeh, variant, 4,
+                [&](int c) { launch_cgm_doe<NR>(kSplCand[c], B, sc, st); }, st);
 }
 
 // s = m2 p - D_eo t ; alpha = <p,s> ; then the shifted recurrences
@@ -790,13 +876,10 @@ void enqueue_cgm_iteration(const CgmBatchBuffers& B, CgmScal* sc, int* snap, cud
   const int bps = seg_blocks(n4, NR);
   ReduceWs ws = reduce_ws(HopLayout<NR>::SLOTS, nb > NR * bps ? nb : NR * bps);
   k_cgm_snapshot<<<1, 32, 0, st>>>(sc, snap);
-  if (B.ph32_mode == PH_SIGN8) {
-    k_cgm_doe<NR, PH_SIGN8><<<nb, BT, 0, st>>>(g, u, B.ph32, B.p, B.t, n, sc);
-    k_cgm_deo_dot<NR, PH_SIGN8><<<nb, BT, 0, st>>>(g, u, B.ph32, B.t, B.p, B.s, n, sc, ws);
-  } else {
-    k_cgm_doe<NR, PH_ANGLE><<<nb, BT, 0, st>>>(g, u, B.ph32, B.p, B.t, n, sc);
-    k_cgm_deo_dot<NR, PH_ANGLE><<<nb, BT, 0, st>>>(g, u, B.ph32, B.t, B.p, B.s, n, sc, ws);
-  }
+  const int pick = autotune_cached(TUNE_CGM_DOE, g.sizeh, NR * 2 + (B.ph32_mode == PH_SIGN8));
+  launch_cgm_doe<NR>(kSplCand[pick > 0 && pick < 4 ? pick : 0], B, sc, st);
+  if (B.ph32_mode == PH_SIGN8) k_cgm_deo_dot<NR, PH_SIGN8><<<nb, BT, 0, st>>>(g, u, B.ph32, B.t, B.p, B.s, n, sc, ws);
+  else k_cgm_deo_dot<NR, PH_ANGLE><<<nb, BT, 0, st>>>(g, u, B.ph32, B.t, B.p, B.s, n, sc, ws);
   k_cgm_r<NR><<<NR * bps, RED_THREADS, 0, st>>>(reinterpret_cast<float4*>(B.r), reinterpret_cast<const float4*>(B.s),
                                                 n4, n4, bps, sc, ws);
   // the x/p update streams nshift+1 fields per side: give it more blocks
@@ -852,6 +935,13 @@ CgmBatchResult batched_cgm_f32(const CgmBatchBuffers& B, double mass2, const dou
   OST_CUDA(cudaStreamSynchronize(st));
   for (int r = 0; r < NR; ++r) { h->delta[r] = hn[r]; h->bnorm2[r] = hn[r]; }
   OST_CUDA(cudaMemcpyAsync(sc, h, sizeof(CgmScal), cudaMemcpyHostToDevice, st));
+  // launch shape of the D_oe (numerics-invariant; t is scratch), chosen before the capture
+  switch (NR) {
+    case 1: tune_cgm_doe<1>(B, st); break;
+    case 2: tune_cgm_doe<2>(B, st); break;
+    case 3: tune_cgm_doe<3>(B, st); break;
+    default: tune_cgm_doe<4>(B, st); break;
+  }
   // capture a chunk of iterations once per call (the buffers change per call)
   const int chunk = 8;
   cudaGraph_t graph;

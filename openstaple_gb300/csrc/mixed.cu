@@ -11,6 +11,7 @@
 // update (need_rel), so replaying a chunk past either point does no work.
 #include <cmath>
 #include <cstring>
+#include "autotune.cuh"
 #include "dslash.cuh"
 #include "kernels.cuh"
 #include "mixed.cuh"
@@ -65,9 +66,10 @@ void phases_to_f32(const double* ph64, float* ph32, long sh, cudaStream_t st) {
 }
 
 // ---- FP32 iteration kernels ----
-// t = D_oe p
+// t = D_oe p (one thread per site, any block size up to 256: the autotuner
+// picks the block size)
 template <int PH>
-__global__ void __launch_bounds__(MX_THREADS)
+__global__ void __launch_bounds__(256)
 k_mx_doe(Geom g, LinkView<float2> u, const void* __restrict__ ph, const float2* __restrict__ p,
          float2* __restrict__ t, const MixScal* sc) {
   if (halted(sc)) return;
@@ -227,6 +229,7 @@ struct GraphCache {
   int chunk = 0;
   MixScal* sc = nullptr;
   unsigned long long epoch = 0;
+  int doe_threads = 0;
 };
 GraphCache g_cache;
 cudaStream_t g_cap = nullptr;
@@ -250,6 +253,37 @@ void fp64_mdagm(const MixedBuffers& B, double2* out, const double2* in, double2*
   launch_dslash<double>(a);
 }
 
+// Block sizes the autotuner tries for k_mx_doe (the first is the default).
+static const int kDoeThreads[3] = {MX_THREADS, 256, 64};
+
+void launch_mx_doe(int threads, const MixedBuffers& B, const MixScal* sc, cudaStream_t st) {
+  const Geom& g = rt().g;
+  LinkView<float2> u{B.u32, g.sizeh, B.u32_compact ? 6 : 9};
+  const int nb = blocks_for(g.sizeh, threads);
+  if (B.ph32_mode == PH_SIGN8) k_mx_doe<PH_SIGN8><<<nb, threads, 0, st>>>(g, u, B.ph32, B.p, B.t, sc);
+  else k_mx_doe<PH_ANGLE><<<nb, threads, 0, st>>>(g, u, B.ph32, B.p, B.t, sc);
+}
+
+int mx_doe_threads(const MixedBuffers& B) {
+  const int pick = autotune_cached(TUNE_MX_DOE, rt().g.sizeh, B.ph32_mode == PH_SIGN8);
+  return kDoeThreads[pick > 0 && pick < 3 ? pick : 0];
+}
+
+// Tunes the k_mx_doe block size once per lattice (t is scratch; the timing
+// launches see a copy of the scalars with the solve running).
+int tune_mx_doe(const MixedBuffers& B, cudaStream_t st) {
+  const int variant = B.ph32_mode == PH_SIGN8;
+  if (autotune_cached(TUNE_MX_DOE, rt().g.sizeh, variant) < 0 && autotune_enabled()) {
+    MixScal h;
+    memset(&h, 0, sizeof(h));
+    const MixScal* sc = static_cast<const MixScal*>(autotune_scalars(&h, sizeof(h), st));
+    if (sc)
+      autotune_pick(TUNE_MX_DOE, rt().g.sizeh, variant, 3,
+                    [&](int c) { launch_mx_doe(kDoeThreads[c], B, sc, st); }, st);
+  }
+  return mx_doe_threads(B);
+}
+
 void enqueue_iteration(const MixedBuffers& B, MixScal* sc, cudaStream_t st) {
   const Geom& g = rt().g;
   LinkView<float2> u{B.u32, g.sizeh, B.u32_compact ? 6 : 9};
@@ -258,13 +292,10 @@ void enqueue_iteration(const MixedBuffers& B, MixScal* sc, cudaStream_t st) {
   int gr = reduce_grid(n4);
   int gd = nb;
   ReduceWs wsd = reduce_ws(1, gd > gr ? gd : gr);
-  if (B.ph32_mode == PH_SIGN8) {
-    k_mx_doe<PH_SIGN8><<<nb, MX_THREADS, 0, st>>>(g, u, B.ph32, B.p, B.t, sc);
+  launch_mx_doe(mx_doe_threads(B), B, sc, st);
+  if (B.ph32_mode == PH_SIGN8)
     k_mx_deo_dot<PH_SIGN8><<<nb, MX_THREADS, 0, st>>>(g, u, B.ph32, B.t, B.p, B.s, sc, wsd);
-  } else {
-    k_mx_doe<PH_ANGLE><<<nb, MX_THREADS, 0, st>>>(g, u, B.ph32, B.p, B.t, sc);
-    k_mx_deo_dot<PH_ANGLE><<<nb, MX_THREADS, 0, st>>>(g, u, B.ph32, B.t, B.p, B.s, sc, wsd);
-  }
+  else k_mx_deo_dot<PH_ANGLE><<<nb, MX_THREADS, 0, st>>>(g, u, B.ph32, B.t, B.p, B.s, sc, wsd);
   g_kernel_launches += 2;
   k_mx_update<<<gr, RED_THREADS, 0, st>>>(reinterpret_cast<float4*>(B.xf), reinterpret_cast<float4*>(B.r),
                                           reinterpret_cast<const float4*>(B.p),
@@ -334,9 +365,11 @@ MixedResult mixed_cg(const MixedBuffers& B, const MixedOptions& o, MixScal* sc, 
     const int gr = reduce_grid(n);
     reduce_ws(2, nb > gr ? nb : gr);
   }
+  // launch shape of the D_oe (numerics-invariant), chosen before the capture
+  const int doe_threads = tune_mx_doe(B, cs);
   // (re)capture the iteration chunk
   if (!g_cache.exec || !same_key(g_cache.key, B) || g_cache.chunk != o.chunk || g_cache.sc != sc ||
-      g_cache.epoch != runtime_epoch()) {
+      g_cache.epoch != runtime_epoch() || g_cache.doe_threads != doe_threads) {
     if (g_cache.exec) cudaGraphExecDestroy(g_cache.exec);
     g_cache.exec = nullptr;
     cudaGraph_t graph;
@@ -351,6 +384,7 @@ MixedResult mixed_cg(const MixedBuffers& B, const MixedOptions& o, MixScal* sc, 
     g_cache.chunk = o.chunk;
     g_cache.sc = sc;
     g_cache.epoch = runtime_epoch();
+    g_cache.doe_threads = doe_threads;
   }
 
   const long n4 = n / 2;
@@ -426,6 +460,7 @@ double time_mixed_kernel(const MixedBuffers& B, MixScal* sc, int which, int reps
   init.delta = 1.0;
   OST_CUDA(cudaMemcpyAsync(sc, &init, sizeof(MixScal), cudaMemcpyHostToDevice, st));
   ReduceWs ws = reduce_ws(1, nb);
+  const int doe_threads = which == 1 ? tune_mx_doe(B, st) : MX_THREADS;
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
@@ -434,8 +469,7 @@ double time_mixed_kernel(const MixedBuffers& B, MixScal* sc, int which, int reps
     cudaEventRecord(e0, st);
     for (int k = 0; k < reps; ++k) {
       if (which == 1) {
-        if (B.ph32_mode == PH_SIGN8) k_mx_doe<PH_SIGN8><<<nb, MX_THREADS, 0, st>>>(g, u, B.ph32, B.p, B.t, sc);
-        else k_mx_doe<PH_ANGLE><<<nb, MX_THREADS, 0, st>>>(g, u, B.ph32, B.p, B.t, sc);
+        launch_mx_doe(doe_threads, B, sc, st);
       } else {
         if (B.ph32_mode == PH_SIGN8)
           k_mx_deo_dot<PH_SIGN8><<<nb, MX_THREADS, 0, st>>>(g, u, B.ph32, B.t, B.p, B.s, sc, ws);

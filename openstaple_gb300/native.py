@@ -102,6 +102,8 @@ SIGNATURES = {
     "ostaple_pin_host": (_I, [_P, C.c_size_t]),
     "ostaple_unpin_host": (_I, [_P]),
     "ostaple_time_kernel": (_I, [_I, _P, _P, _I, C.POINTER(_D)]),
+    "ostaple_autotune": (_I, [_I]),
+    "ostaple_autotune_report": (_I, [C.c_char_p, _I]),
     "acc_Deo": (None, [_P, _P, _P, _P]),
     "acc_Doe": (None, [_P, _P, _P, _P]),
     "acc_Deo_unsafe": (None, [_P, _P, _P, _P]),
