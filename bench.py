@@ -44,6 +44,9 @@ FALLBACK_HBM = 6800.0
 BYTES_F32_SIGN = 8 * 12 * 4 + 8 * 1 + 3 * 8 + 3 * 8      # = 440
 # D_eo + M^+M epilogue + <p,s> per output site: links + sign bytes + t and p in + s out
 BYTES_F32_DEO = 8 * 12 * 4 + 8 * 1 + 2 * 3 * 8 + 3 * 8        # = 464
+# the same with the links in 16-bit fixed point (12 x 2 bytes per link)
+BYTES_Q16_SIGN = 8 * 12 * 2 + 8 * 1 + 3 * 8 + 3 * 8      # = 248
+BYTES_Q16_DEO = 8 * 12 * 2 + 8 * 1 + 2 * 3 * 8 + 3 * 8        # = 272
 BYTES_F64_ANGLE = 8 * 12 * 8 + 8 * 8 + 3 * 16 + 3 * 16   # links(2 rows) + angles + in + out = 928
 
 
@@ -67,6 +70,8 @@ def parse_args():
     ap.add_argument("--train-epochs", type=int, default=150)
     ap.add_argument("--rhs", type=int, default=1,
                     help="right-hand sides per step; >1 solves them together with the batched solver")
+    ap.add_argument("--links", choices=("q16", "f32"), default="q16",
+                    help="sloppy link format of the FP32 iteration (16-bit fixed point or FP32 rows)")
     ap.add_argument("--delta", type=float, default=1e-4,
                     help="reliable update when |r|^2 < delta * max|r|^2 since the last one")
     return ap.parse_args()
@@ -225,6 +230,8 @@ def main():
     dims = tuple(int(x) for x in args.dims.split(","))
     u, ph, b = make_inputs(dims, args.seed + 17 * rank, args.eps)
     lat = api.Lattice(dims)
+    api.set_sloppy_links(args.links)
+    bytes_deo, bytes_doe = (BYTES_Q16_DEO, BYTES_Q16_SIGN) if args.links == "q16" else (BYTES_F32_DEO, BYTES_F32_SIGN)
     stream = torch.cuda.Stream()
     L.ostaple_set_stream(C.c_void_p(stream.cuda_stream))
     x = lat.vec3()
@@ -339,16 +346,17 @@ def main():
     hbm, peak_kind = peaks()
     kms = C.c_double(0)
     L.ostaple_time_kernel(2, u.ctypes.data, ph.ctypes.data, 50, C.byref(kms))
-    achieved = BYTES_F32_DEO * lat.sizeh / (kms.value * 1e-3) / 1e9
+    achieved = bytes_deo * lat.sizeh / (kms.value * 1e-3) / 1e9
     kdoe = C.c_double(0)
     L.ostaple_time_kernel(1, u.ctypes.data, ph.ctypes.data, 50, C.byref(kdoe))
-    achieved_doe = BYTES_F32_SIGN * lat.sizeh / (kdoe.value * 1e-3) / 1e9
+    achieved_doe = bytes_doe * lat.sizeh / (kdoe.value * 1e-3) / 1e9
     traffic, traffic_doe = None, None
     if PROFILE_TRAFFIC.exists():
         tr = json.loads(PROFILE_TRAFFIC.read_text())
         tag = 'x'.join(map(str, dims))
-        traffic = tr.get(f"dslash_f32_deo_dot_{tag}", {}).get("bytes_per_launch")
-        traffic_doe = tr.get(f"dslash_f32_doe_{tag}", {}).get("bytes_per_launch")
+        fam = "q16" if args.links == "q16" else "f32"
+        traffic = tr.get(f"dslash_{fam}_deo_dot_{tag}", {}).get("bytes_per_launch")
+        traffic_doe = tr.get(f"dslash_{fam}_doe_{tag}", {}).get("bytes_per_launch")
     k64 = C.c_double(0)
     L.ostaple_time_kernel(0, u.ctypes.data, ph.ctypes.data, 10, C.byref(k64))
     fp64_peak = C.c_double(0)
@@ -401,6 +409,7 @@ def main():
                                   "mixed-precision CG (FP32 iteration, double-float reliable updates, FP64 final "
                                   "residual, CUDA-graph chunks)" if nrhs == 1 else
                                   f"batched mixed-precision CG, {nrhs} right-hand sides sharing each link load"),
+                       "sloppy_links": args.links,
                        "learned": learned,
                        "rhs_per_step": nrhs,
                        "batched_4rhs": batched4,
@@ -410,12 +419,14 @@ def main():
                        "speedup_vs_plain_fp64_cg": fp64["ms"] * nrhs / ms if fp64["ms"] else None,
                        "l2": "inputs larger than L2 (FP32 links 201 MB, FP64 links 604 MB > 129 MB)",
                        "parallelism": f"replicas x{world}"},
-            "roofline": {"kernel": "k_mx_deo_dot (FP32 D_eo + M^+M epilogue + <p,Ap>, compact links + sign bytes)",
+            "roofline": {"kernel": "k_mx_deo_dot (FP32 D_eo + M^+M epilogue + <p,Ap>, "
+                                   + ("16-bit fixed-point links" if args.links == "q16" else "FP32 two-row links")
+                                   + " + sign bytes)",
                          "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                          "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
-                         "traffic": traffic, "bytes_per_site": BYTES_F32_DEO, "ms_per_launch": kms.value,
+                         "traffic": traffic, "bytes_per_site": bytes_deo, "ms_per_launch": kms.value,
                          "doe": {"kernel": "k_mx_doe (FP32 D_oe)", "achieved": achieved_doe,
-                                 "frac": achieved_doe / hbm, "traffic": traffic_doe, "bytes_per_site": BYTES_F32_SIGN,
+                                 "frac": achieved_doe / hbm, "traffic": traffic_doe, "bytes_per_site": bytes_doe,
                                  "ms_per_launch": kdoe.value}},
             "fp64_dslash": {"ms_per_launch": k64.value,
                             "hbm_gbs": BYTES_F64_ANGLE * lat.sizeh / (k64.value * 1e-3) / 1e9,

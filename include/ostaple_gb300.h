@@ -306,6 +306,22 @@ void find_min_max_eigenvalue_soloopenacc(const su3_soa *u, ferm_param *pars, vec
 int ostaple_mdagm_df(const su3_soa *u, const double_soa *phases, double mass, double shift, vec3_soa *out,
                      const vec3_soa *in);
 
+/* Link format of the FP32 iteration of the mixed and batched solvers when
+ * the library converts the FP64 links itself: fmt = 1 (default) the first
+ * two rows in 16-bit fixed point (24 bytes per link, absolute error <= 2^-16;
+ * the reliable updates and the FP64 closing residual keep every solution at
+ * the requested FP64 residual), fmt = 0 two FP32 rows (48 bytes per link).
+ * Returns the previous format.  Links passed by the caller as su3_soa_f
+ * (inverter_package.u_f) are always used as given.  No reference
+ * counterpart (the reference's sloppy links are FP32). */
+int ostaple_set_sloppy_links(int fmt);
+/* out = (m^2 + shift) in - D_eo D_oe in through the FP32 iteration kernels
+ * with the current sloppy link format (FP32 in and out of the kernels, FP64
+ * fields here): the operator of the FP32 iteration, exposed for testing.
+ * No reference counterpart. */
+int ostaple_mdagm_sloppy(const su3_soa *u, const double_soa *phases, double mass, double shift, vec3_soa *out,
+                         const vec3_soa *in);
+
 /* Mixed-precision CG: FP32 iteration, FP64 solution and reliable updates of
  * the residual when |r|^2 < inverter_tricks.mixedPrecisionDelta * max|r|^2
  * (inverter_mixedp.c:41-48).  FP32 links come from ip.u_f when set (the

@@ -127,6 +127,20 @@ def mdagm_df(u, phases, mass: float, out, inp, shift: float = 0.0) -> None:
     check(lib().ostaple_mdagm_df(ptr(u), ptr(phases), mass, shift, ptr(out), ptr(inp)), "ostaple_mdagm_df")
 
 
+def set_sloppy_links(fmt: str) -> str:
+    """Link format of the FP32 iteration: "q16" (16-bit fixed point, the
+    default) or "f32"; returns the previous one."""
+    if fmt not in ("q16", "f32"):
+        raise ValueError(f"sloppy link format must be 'q16' or 'f32', not {fmt!r}")
+    prev = lib().ostaple_set_sloppy_links(1 if fmt == "q16" else 0)
+    return "q16" if prev else "f32"
+
+
+def mdagm_sloppy(u, phases, mass: float, out, inp, shift: float = 0.0) -> None:
+    """out = (m^2 + shift) inp - D_eo D_oe inp through the FP32 iteration kernels."""
+    check(lib().ostaple_mdagm_sloppy(ptr(u), ptr(phases), mass, shift, ptr(out), ptr(inp)), "ostaple_mdagm_sloppy")
+
+
 def l2norm2_global(v) -> float:
     r = lib().l2norm2_global(ptr(v))
     check(0, "l2norm2_global")

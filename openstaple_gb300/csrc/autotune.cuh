@@ -17,7 +17,7 @@
 
 namespace ost {
 
-enum TuneKernel { TUNE_MX_DOE = 0, TUNE_B_DOE = 1, TUNE_CGM_DOE = 2 };
+enum TuneKernel { TUNE_MX_DOE = 0, TUNE_B_DOE = 1, TUNE_CGM_DOE = 2, TUNE_MX_DEO = 3 };
 
 bool autotune_enabled();
 

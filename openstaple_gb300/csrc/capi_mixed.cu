@@ -22,7 +22,11 @@ struct PreparedF32 {
   int compact;
   const void* ph;
   int mode;
+  int q16;
+  LinkQ16 uq;
 };
+
+int g_sloppy_q16 = 1;
 
 // FP32 links and phases for the single-precision kernels.  Links: the
 // caller's su3_soa_f if given, else a compact conversion of the FP64 links.
@@ -30,6 +34,8 @@ struct PreparedF32 {
 // angles.
 bool prepare_f32(const Z* u64, const void* u_f, const double* ph64, PreparedF32* out, cudaStream_t st) {
   const long sh = rt().g.sizeh;
+  out->q16 = 0;
+  out->uq = LinkQ16{nullptr, nullptr, sh};
   if (u_f) {
     out->u32 = static_cast<const float2*>(resolve(u_f, "u_f"));
     if (!out->u32) return false;
@@ -40,6 +46,16 @@ bool prepare_f32(const Z* u64, const void* u_f, const double* ph64, PreparedF32*
     links_to_f32_compact(u64, u32, sh, st);
     out->u32 = u32;
     out->compact = 1;
+    if (g_sloppy_q16) {
+      // 8 directions x (16 + 8) bytes per half-lattice site
+      char* q = static_cast<char*>(workspace(WS_LINKS_Q16, 8 * 24 * size_t(sh)));
+      if (!q) return false;
+      uint4* a = reinterpret_cast<uint4*>(q);
+      uint2* b = reinterpret_cast<uint2*>(q + 8 * 16 * size_t(sh));
+      links_to_q16(u64, a, b, sh, st);
+      out->q16 = 1;
+      out->uq = LinkQ16{a, b, sh};
+    }
   }
   char* sg = static_cast<char*>(workspace(WS_SIGNS, 256 + 8 * size_t(sh) * sizeof(float)));
   if (!sg) return false;
@@ -83,7 +99,47 @@ MixScal* mix_scalars() {
 
 }  // namespace
 
+namespace ost {
+int sloppy_links_q16() { return g_sloppy_q16; }
+}  // namespace ost
+
 extern "C" {
+
+int ostaple_set_sloppy_links(int fmt) {
+  const int prev = g_sloppy_q16;
+  g_sloppy_q16 = fmt ? 1 : 0;
+  return prev;
+}
+
+int ostaple_mdagm_sloppy(const su3_soa* u, const double_soa* phases, double mass, double shift, vec3_soa* out,
+                         const vec3_soa* in) {
+  if (!require_init("ostaple_mdagm_sloppy")) return -2;
+  cudaStream_t st = rt().stream;
+  const Z* u64 = dev(reinterpret_cast<const Z*>(u), "u");
+  const void* ph = resolve(phases, "phases");
+  const Z* din = dev(reinterpret_cast<const Z*>(in), "in");
+  Z* dout = dev(reinterpret_cast<Z*>(out), "out");
+  if (!u64 || !ph || !din || !dout) return -3;
+  MixedBuffers B{};
+  B.u64 = u64;
+  B.ph64 = ph;
+  B.t = ws_vec<Zf>(WS_VEC1, 1, 5);
+  B.s = ws_vec<Zf>(WS_VEC1, 2, 5);
+  B.p = ws_vec<Zf>(WS_VEC1, 3, 5);
+  if (!B.t || !B.s || !B.p) return -4;
+  PreparedF32 pf;
+  if (!prepare_f32(u64, nullptr, static_cast<const double*>(ph), &pf, st)) return -4;
+  B.u32 = pf.u32;
+  B.u32_compact = pf.compact;
+  B.q16 = pf.q16;
+  B.uq = pf.uq;
+  B.ph32 = pf.ph;
+  B.ph32_mode = pf.mode;
+  MixScal* sc = mix_scalars();
+  if (!sc) return -4;
+  sloppy_mdagm(B, mass * mass + shift, din, dout, sc + 1, st);
+  return error_code();
+}
 
 int inverter_mixed_precision(inverter_package ip, ferm_param* pars, vec3_soa* solution, const vec3_soa* in,
                              double res, const int max_cg, double shift, int* cg_return) {
@@ -110,6 +166,8 @@ int inverter_mixed_precision(inverter_package ip, ferm_param* pars, vec3_soa* so
   if (!prepare_f32(B.u64, ip.u_f, static_cast<const double*>(B.ph64), &pf, st)) return INVERTER_FAILURE;
   B.u32 = pf.u32;
   B.u32_compact = pf.compact;
+  B.q16 = pf.q16;
+  B.uq = pf.uq;
   B.ph32 = pf.ph;
   B.ph32_mode = pf.mode;
   B.use_df = prepare_df(B.u64, pf, &B.df, &B.dfw, st) ? 1 : 0;
@@ -155,6 +213,8 @@ int ostaple_invert_mixed(const su3_soa* u, const double_soa* phases, double mass
   if (!prepare_f32(B.u64, nullptr, static_cast<const double*>(B.ph64), &pf, st)) return INVERTER_FAILURE;
   B.u32 = pf.u32;
   B.u32_compact = pf.compact;
+  B.q16 = pf.q16;
+  B.uq = pf.uq;
   B.ph32 = pf.ph;
   B.ph32_mode = pf.mode;
   B.use_df = prepare_df(B.u64, pf, &B.df, &B.dfw, st) ? 1 : 0;
@@ -245,6 +305,8 @@ int ostaple_time_kernel(int which, const su3_soa* u, const double_soa* phases, i
   if (!prepare_f32(u64, nullptr, static_cast<const double*>(ph), &pf, st)) return -4;
   B.u32 = pf.u32;
   B.u32_compact = pf.compact;
+  B.q16 = pf.q16;
+  B.uq = pf.uq;
   B.ph32 = pf.ph;
   B.ph32_mode = pf.mode;
   MixScal* sc = mix_scalars();

@@ -89,6 +89,42 @@ OST_D void load_two_rows(const LinkView<C>& u, int dir, int idx, C m[6]) {
   for (int k = 0; k < 6; ++k) m[k] = __ldcs(u.at(dir, k / 3, k % 3) + idx);
 }
 
+// Sloppy links in 16-bit fixed point: the first two rows of each link,
+// every real and imaginary part q = rint(32768 x) clamped to +-32767 and
+// stored biased as q + 32768 in 16 bits (real part in the low half of a
+// 32-bit word, imaginary part in the high half).  SU(3) entries lie in
+// [-1, 1], so the absolute error is at most 2^-16.  Per direction two
+// planes over the half lattice: `a` holds elements 0-3 of rows 0-1
+// (16 bytes), `b` elements 4-5 (8 bytes), so one link is 24 bytes against
+// 48 for two FP32 rows.  Decoding: the bit pattern 0x4B000000 | u is the
+// float 2^23 + u, and (2^23 + u) * 2^-15 - 257 = (u - 32768) / 32768 is exact
+// in one FMA.
+struct LinkQ16 {
+  const uint4* a;
+  const uint2* b;
+  long sizeh;
+};
+
+OST_D float2 q16_decode(unsigned w) {
+  const float lo = __int_as_float(int(0x4B000000u | (w & 0xFFFFu)));
+  const float hi = __int_as_float(int(0x4B000000u | (w >> 16)));
+  return make_float2(fmaf(lo, 3.0517578125e-05f, -257.0f), fmaf(hi, 3.0517578125e-05f, -257.0f));
+}
+
+OST_HD unsigned q16_encode_part(double x) {
+  double q = rint(x * 32768.0);
+  q = q > 32767.0 ? 32767.0 : (q < -32767.0 ? -32767.0 : q);
+  return unsigned(int(q) + 32768);
+}
+
+OST_D void load_two_rows(const LinkQ16& u, int dir, int idx, float2 m[6]) {
+  const long k = long(dir) * u.sizeh + idx;
+  const uint4 a = __ldcs(u.a + k);
+  const uint2 b = __ldcs(u.b + k);
+  m[0] = q16_decode(a.x); m[1] = q16_decode(a.y); m[2] = q16_decode(a.z);
+  m[3] = q16_decode(a.w); m[4] = q16_decode(b.x); m[5] = q16_decode(b.y);
+}
+
 // aux += U v (U rebuilt from two rows)
 template <typename C>
 OST_D void mac_U(C aux[3], const C m[6], const C v[3]) {
@@ -125,11 +161,54 @@ struct PhaseView {
   long sizeh;
 };
 
-// The hop term at output index idx of parity P.
-template <typename T, int P, int PH>
-OST_D void hop(const Geom& g, const LinkView<typename cplx_t<T>::type>& u,
-               const typename cplx_t<T>::type* in, const void* phases, int idx,
+// An empty asm statement that consumes a value: the value must be
+// available at this point of the program.
+OST_D void pin_value(float v) { asm volatile("" ::"f"(v)); }
+OST_D void pin_value(double v) { asm volatile("" ::"d"(v)); }
+OST_D void pin_value(float2 v) { asm volatile("" ::"f"(v.x), "f"(v.y)); }
+OST_D void pin_value(double2 v) { asm volatile("" ::"d"(v.x), "d"(v.y)); }
+OST_D void pin_value(unsigned char v) { asm volatile("" ::"r"(unsigned(v))); }
+
+// Raw link words as loaded (before decoding), per link view type.
+template <typename LV> struct LinkRaw;
+template <typename C> struct LinkRaw<LinkView<C>> {
+  C m[6];
+  OST_D void load(const LinkView<C>& u, int dir, int idx) { load_two_rows(u, dir, idx, m); }
+  OST_D void rows(C out[6]) const {
+#pragma unroll
+    for (int k = 0; k < 6; ++k) out[k] = m[k];
+  }
+  OST_D void pin() const {
+#pragma unroll
+    for (int k = 0; k < 6; ++k) pin_value(m[k]);
+  }
+};
+template <> struct LinkRaw<LinkQ16> {
+  uint4 a;
+  uint2 b;
+  OST_D void load(const LinkQ16& u, int dir, int idx) {
+    const long k = long(dir) * u.sizeh + idx;
+    a = __ldcs(u.a + k);
+    b = __ldcs(u.b + k);
+  }
+  OST_D void rows(float2 m[6]) const {
+    m[0] = q16_decode(a.x); m[1] = q16_decode(a.y); m[2] = q16_decode(a.z);
+    m[3] = q16_decode(a.w); m[4] = q16_decode(b.x); m[5] = q16_decode(b.y);
+  }
+  OST_D void pin() const { asm volatile("" ::"r"(a.x), "r"(a.y), "r"(a.z), "r"(a.w), "r"(b.x), "r"(b.y)); }
+};
+
+// The hop term at output index idx of parity P: aux = sum over the four
+// backward hops -e^{-i th} U_b(x-mu)^+ in(x-mu), then the four forward hops
+// e^{i th} U_f(x) in(x+mu), accumulated in that order.  The loads (link,
+// input, phase) of HB consecutive hops are issued before their arithmetic;
+// HB changes how many loads a thread keeps in flight, never the arithmetic
+// or its order, so every HB gives the same bits.  LV is LinkView<C> (FP64
+// or FP32 rows) or LinkQ16 (FP32 arithmetic only).
+template <typename T, int P, int PH, typename LV, int HB = 1>
+OST_D void hop(const Geom& g, const LV& u, const typename cplx_t<T>::type* in, const void* phases, int idx,
                typename cplx_t<T>::type aux[3]) {
+  static_assert(8 % HB == 0, "hops in flight must divide 8");
   typedef typename cplx_t<T>::type C;
   typedef typename SignMask<T>::type M;
   const long sh = g.sizeh;
@@ -138,48 +217,174 @@ OST_D void hop(const Geom& g, const LinkView<typename cplx_t<T>::type>& u,
   neighbours(g, s, fwd, bwd);
 #pragma unroll
   for (int c = 0; c < 3; ++c) aux[c] = cmk<C>(T(0), T(0));
-
-  // backward hops: aux -= e^{-i th} U_b(x-mu)^+ in(x-mu)
 #pragma unroll
-  for (int mu = 0; mu < 4; ++mu) {
-    const int dir = 2 * mu + (1 - P);
-    const int j = bwd[mu];
-    C m[6], v[3];
-    load_two_rows(u, dir, j, m);
-    load_vec(in, sh, j, v);
-    if (PH == PH_ANGLE) {
-      T arg = __ldcs(static_cast<const T*>(phases) + long(dir) * sh + j);
-      apply_angle_phase<T, true>(v, arg, SignMask<T>::neg);
-    } else if (PH == PH_SIGN8) {
-      unsigned char sb = __ldg(static_cast<const unsigned char*>(phases) + long(dir) * sh + j);
-      M mask = (sb ? M(0) : SignMask<T>::neg);
+  for (int h0 = 0; h0 < 8; h0 += HB) {
+    LinkRaw<LV> raw[HB];
+    C v[HB][3];
+    T arg[HB];
+    unsigned char sb[HB];
+#pragma unroll
+    for (int k = 0; k < HB; ++k) {
+      const int hm = h0 + k;
+      const bool back = hm < 4;                 // backward hops first, as in the reference
+      const int mu = hm & 3;
+      const int dir = back ? 2 * mu + (1 - P) : 2 * mu + P;
+      const int j = back ? bwd[mu] : fwd[mu];   // input site
+      const int l = back ? j : idx;             // link site
+      raw[k].load(u, dir, l);
+      load_vec(in, sh, j, v[k]);
+      if (PH == PH_ANGLE) arg[k] = __ldcs(static_cast<const T*>(phases) + long(dir) * sh + l);
+      else if (PH == PH_SIGN8) sb[k] = __ldg(static_cast<const unsigned char*>(phases) + long(dir) * sh + l);
+    }
+    // the batch's loaded values all pass through one empty asm statement, so
+    // every load of the batch is issued before the first hop's arithmetic
+    // (otherwise the compiler may sink each load to its first use)
+    if (HB > 1) {
+#pragma unroll
+      for (int k = 0; k < HB; ++k) {
+        raw[k].pin();
+#pragma unroll
+        for (int c = 0; c < 3; ++c) pin_value(v[k][c]);
+        if (PH == PH_ANGLE) pin_value(arg[k]);
+        else if (PH == PH_SIGN8) pin_value(sb[k]);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < HB; ++k) {
+      const bool back = h0 + k < 4;
+      if (PH == PH_ANGLE) {
+        if (back) apply_angle_phase<T, true>(v[k], arg[k], SignMask<T>::neg);
+        else apply_angle_phase<T, false>(v[k], arg[k], M(0));
+      } else if (PH == PH_SIGN8) {
+        const M mask = back ? (sb[k] ? M(0) : SignMask<T>::neg) : (sb[k] ? SignMask<T>::neg : M(0));
+#pragma unroll
+        for (int c = 0; c < 3; ++c) { v[k][c].x = flip_sign(v[k][c].x, mask); v[k][c].y = flip_sign(v[k][c].y, mask); }
+      } else if (back) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) { v[k][c].x = -v[k][c].x; v[k][c].y = -v[k][c].y; }
+      }
+      C m[6];
+      raw[k].rows(m);
+      if (back) mac_Udag(aux, m, v[k]);
+      else mac_U(aux, m, v[k]);
+    }
+  }
+}
+
+// ---- FP32 hop term with the backward and forward sums kept apart ----
+//
+// aux = B + F with B = sum over the four backward hops and F over the four
+// forward hops, each accumulated in hop order (two independent FMA chains
+// instead of one).  A backward hop adds U^+ v as sum_j cmac(conj(U_ji), v_j),
+// which is exactly mac_Udag's cmacc(U_ji, v_j).  Every HB gives the same
+// bits.
+
+// the phase of a hop applied to v (back: the conjugate phase and the minus
+// sign of the backward term)
+template <int PH>
+OST_D void apply_hop_phase(float2 v[3], bool back, float arg, unsigned char sb) {
+  typedef SignMask<float>::type M;
+  if (PH == PH_ANGLE) {
+    const M extra = back ? SignMask<float>::neg : M(0);
+    const M bits = __float_as_uint(arg);
+    if (bits == 0 || bits == PiBits<float>::bits()) {
+      const M mask = (bits == 0 ? M(0) : SignMask<float>::neg) ^ extra;
 #pragma unroll
       for (int c = 0; c < 3; ++c) { v[c].x = flip_sign(v[c].x, mask); v[c].y = flip_sign(v[c].y, mask); }
     } else {
+      float sn, co;
+      sincosf(arg, &sn, &co);
+      const float2 ph = make_float2(co, back ? -sn : sn);
 #pragma unroll
-      for (int c = 0; c < 3; ++c) { v[c].x = -v[c].x; v[c].y = -v[c].y; }
+      for (int c = 0; c < 3; ++c) {
+        v[c] = cmul(v[c], ph);
+        v[c].x = flip_sign(v[c].x, extra); v[c].y = flip_sign(v[c].y, extra);
+      }
     }
-    mac_Udag(aux, m, v);
+  } else {
+    M mask;
+    if (PH == PH_SIGN8) mask = back ? (sb ? M(0) : SignMask<float>::neg) : (sb ? SignMask<float>::neg : M(0));
+    else mask = back ? SignMask<float>::neg : M(0);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) { v[c].x = flip_sign(v[c].x, mask); v[c].y = flip_sign(v[c].y, mask); }
   }
-  // forward hops: aux += e^{i th} U_f(x) in(x+mu)
+}
+
+// acc += W v with W = U (forward) or U^+ (backward), U rebuilt from rows m
+OST_D void mac_hop(float2 acc[3], const float2 m[6], const float2 v[3], bool back) {
+  const float2 r20 = conj_cross(m[1], m[5], m[2], m[4]);
+  const float2 r21 = conj_cross(m[2], m[3], m[0], m[5]);
+  const float2 r22 = conj_cross(m[0], m[4], m[1], m[3]);
+  const float2 u[3][3] = {{m[0], m[1], m[2]}, {m[3], m[4], m[5]}, {r20, r21, r22}};
+  const SignMask<float>::type cm = back ? SignMask<float>::neg : 0u;
 #pragma unroll
-  for (int mu = 0; mu < 4; ++mu) {
-    const int dir = 2 * mu + P;
-    const int j = fwd[mu];
-    C m[6], v[3];
-    load_two_rows(u, dir, idx, m);
-    load_vec(in, sh, j, v);
-    if (PH == PH_ANGLE) {
-      T arg = __ldcs(static_cast<const T*>(phases) + long(dir) * sh + idx);
-      apply_angle_phase<T, false>(v, arg, M(0));
-    } else if (PH == PH_SIGN8) {
-      unsigned char sb = __ldg(static_cast<const unsigned char*>(phases) + long(dir) * sh + idx);
-      M mask = (sb ? SignMask<T>::neg : M(0));
+  for (int i = 0; i < 3; ++i)
 #pragma unroll
-      for (int c = 0; c < 3; ++c) { v[c].x = flip_sign(v[c].x, mask); v[c].y = flip_sign(v[c].y, mask); }
+    for (int j = 0; j < 3; ++j) {
+      float2 w = back ? u[j][i] : u[i][j];
+      w.y = flip_sign(w.y, cm);
+      cmac(acc[i], w, v[j]);
     }
-    mac_U(aux, m, v);
+}
+
+// the four hops of one kind (back: hops 0-3, else 4-7) added to acc,
+// HB hops' loads issued before their arithmetic
+template <int P, int PH, typename LV, int HB>
+OST_D void hop4(const LV& u, const float2* in, const void* phases, long sh, int idx, const int fwd[4],
+                const int bwd[4], bool back, float2 acc[3]) {
+  static_assert(4 % HB == 0, "hops in flight must divide 4");
+#pragma unroll
+  for (int h0 = 0; h0 < 4; h0 += HB) {
+    LinkRaw<LV> raw[HB];
+    float2 v[HB][3];
+    float arg[HB];
+    unsigned char sb[HB];
+#pragma unroll
+    for (int k = 0; k < HB; ++k) {
+      const int mu = h0 + k;
+      const int dir = back ? 2 * mu + (1 - P) : 2 * mu + P;
+      const int j = back ? bwd[mu] : fwd[mu];   // input site
+      const int l = back ? j : idx;             // link site
+      raw[k].load(u, dir, l);
+      load_vec(in, sh, j, v[k]);
+      arg[k] = 0.f;
+      sb[k] = 0;
+      if (PH == PH_ANGLE) arg[k] = __ldcs(static_cast<const float*>(phases) + long(dir) * sh + l);
+      else if (PH == PH_SIGN8) sb[k] = __ldg(static_cast<const unsigned char*>(phases) + long(dir) * sh + l);
+    }
+    if (HB > 1) {
+#pragma unroll
+      for (int k = 0; k < HB; ++k) {
+        raw[k].pin();
+#pragma unroll
+        for (int c = 0; c < 3; ++c) pin_value(v[k][c]);
+        if (PH == PH_ANGLE) pin_value(arg[k]);
+        else if (PH == PH_SIGN8) pin_value(sb[k]);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < HB; ++k) {
+      apply_hop_phase<PH>(v[k], back, arg[k], sb[k]);
+      float2 m[6];
+      raw[k].rows(m);
+      mac_hop(acc, m, v[k], back);
+    }
   }
+}
+
+template <int P, int PH, typename LV, int HB>
+OST_D void hop_fb(const Geom& g, const LV& u, const float2* in, const void* phases, int idx, float2 aux[3]) {
+  const long sh = g.sizeh;
+  Site s = site_of(g, idx, P);
+  int fwd[4], bwd[4];
+  neighbours(g, s, fwd, bwd);
+  float2 accb[3], accf[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) accb[c] = accf[c] = make_float2(0.f, 0.f);
+  hop4<P, PH, LV, HB>(u, in, phases, sh, idx, fwd, bwd, true, accb);
+  hop4<P, PH, LV, HB>(u, in, phases, sh, idx, fwd, bwd, false, accf);
+#pragma unroll
+  for (int c = 0; c < 3; ++c) aux[c] = cadd(accb[c], accf[c]);
 }
 
 }  // namespace ost

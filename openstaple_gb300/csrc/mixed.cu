@@ -11,6 +11,7 @@
 // update (need_rel), so replaying a chunk past either point does no work.
 #include <cmath>
 #include <cstring>
+#include <type_traits>
 #include "autotune.cuh"
 #include "dslash.cuh"
 #include "kernels.cuh"
@@ -36,6 +37,26 @@ __global__ void k_links_f32(const double2* __restrict__ u64, float2* __restrict_
 
 void links_to_f32_compact(const double2* u64, float2* u32, long sh, cudaStream_t st) {
   k_links_f32<<<8 * rt().num_sms, 256, 0, st>>>(u64, u32, sh);
+  OST_LAUNCH_CHECK();
+}
+
+__global__ void k_links_q16(const double2* __restrict__ u64, uint4* __restrict__ a, uint2* __restrict__ b, long sh) {
+  const long n = 8L * sh;
+  for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n; i += long(gridDim.x) * blockDim.x) {
+    const long dir = i / sh, idx = i - dir * sh;
+    unsigned w[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+      const double2 v = __ldcs(u64 + (dir * 9 + k) * sh + idx);
+      w[k] = q16_encode_part(v.x) | (q16_encode_part(v.y) << 16);
+    }
+    a[i] = make_uint4(w[0], w[1], w[2], w[3]);
+    b[i] = make_uint2(w[4], w[5]);
+  }
+}
+
+void links_to_q16(const double2* u64, uint4* a, uint2* b, long sh, cudaStream_t st) {
+  k_links_q16<<<8 * rt().num_sms, 256, 0, st>>>(u64, a, b, sh);
   OST_LAUNCH_CHECK();
 }
 
@@ -66,33 +87,34 @@ void phases_to_f32(const double* ph64, float* ph32, long sh, cudaStream_t st) {
 }
 
 // ---- FP32 iteration kernels ----
-// t = D_oe p (one thread per site, any block size up to 256: the autotuner
-// picks the block size)
-template <int PH>
+// One thread per site; HB hops' loads in flight per thread.
+
+// t = D_oe p (any block size up to 256: the autotuner picks the shape)
+template <int PH, typename LV, int HB>
 __global__ void __launch_bounds__(256)
-k_mx_doe(Geom g, LinkView<float2> u, const void* __restrict__ ph, const float2* __restrict__ p,
-         float2* __restrict__ t, const MixScal* sc) {
+k_mx_doe(Geom g, LV u, const void* __restrict__ ph, const float2* __restrict__ p, float2* __restrict__ t,
+         const MixScal* sc) {
   if (halted(sc)) return;
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= g.sizeh) return;
   float2 aux[3];
-  hop<float, 1, PH>(g, u, p, ph, idx, aux);
+  hop_fb<1, PH, LV, HB>(g, u, p, ph, idx, aux);
 #pragma unroll
   for (int c = 0; c < 3; ++c) t[c * long(g.sizeh) + idx] = make_float2(0.5f * aux[c].x, 0.5f * aux[c].y);
 }
 
 // s = m2 p - D_eo t ; pAp = Re<p, s> ; alpha = delta / pAp
-template <int PH>
+template <int PH, typename LV, int HB>
 __global__ void __launch_bounds__(MX_THREADS)
-k_mx_deo_dot(Geom g, LinkView<float2> u, const void* __restrict__ ph, const float2* __restrict__ t,
-             const float2* __restrict__ p, float2* __restrict__ s, MixScal* sc, ReduceWs ws) {
+k_mx_deo_dot(Geom g, LV u, const void* __restrict__ ph, const float2* __restrict__ t, const float2* __restrict__ p,
+             float2* __restrict__ s, MixScal* sc, ReduceWs ws) {
   if (halted(sc)) return;
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
   float v[1] = {0.0f};
   if (idx < g.sizeh) {
     const float m2 = float(sc->m2);
     float2 aux[3];
-    hop<float, 0, PH>(g, u, t, ph, idx, aux);
+    hop_fb<0, PH, LV, HB>(g, u, t, ph, idx, aux);
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       const long k = c * long(g.sizeh) + idx;
@@ -187,30 +209,46 @@ __global__ void k_mx_accumulate(double2* __restrict__ x, float2* __restrict__ xf
 
 // r64 = b - Ax ; r = (float) r64 ; lambda = |r|^2 ; true_r2 = |r64|^2
 // mode 0: initial (p = r, delta = lambda); mode 1: reliable update
-// (beta = lambda/delta, delta = lambda, last_max = 0).
+// (delta = lambda, last_max = 0, and beta for p = r + beta p below).
+//
+// The reference's reliable update keeps beta = lambda/delta
+// (inverter_mixedp.c:124-150).  That formula assumes the new residual is
+// the recursed one; a recomputed residual that differs from it by more than
+// the recursion's own progress (a late update, or sloppy links coarser than
+// FP32) then makes beta large and the next direction repeats the last one,
+// which can stall the solve.  Here beta = -<r, s>/<p, s> with s = A p of the
+// last iteration (Hestenes-Stiefel), which keeps the next direction
+// A-conjugate to the last one whatever the size of the correction; with
+// FP32 links it gives the same iteration counts as the reference's formula.
 __global__ void k_mx_residual(const double2* __restrict__ b, const double2* __restrict__ ax, double2* __restrict__ r64,
-                              float2* __restrict__ r, float2* __restrict__ p, long n, MixScal* sc, ReduceWs ws,
-                              int mode) {
-  double v[2] = {0.0, 0.0};
+                              float2* __restrict__ r, float2* __restrict__ p, const float2* __restrict__ s, long n,
+                              MixScal* sc, ReduceWs ws, int mode) {
+  double v[3] = {0.0, 0.0, 0.0};
   for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n; i += long(gridDim.x) * blockDim.x) {
     double2 bb = b[i], a = ax[i];
     double2 d = make_double2(bb.x - a.x, bb.y - a.y);
     r64[i] = d;
     float2 f = make_float2(float(d.x), float(d.y));
     r[i] = f;
-    if (mode == 0) p[i] = f;
+    if (mode == 0) {
+      p[i] = f;
+    } else {
+      const float2 sv = s[i];
+      v[2] += double(f.x) * sv.x + double(f.y) * sv.y;
+    }
     v[0] += double(f.x) * f.x + double(f.y) * f.y;
     v[1] += d.x * d.x + d.y * d.y;
   }
-  double tot[2];
-  if (grid_reduce<2>(v, ws, tot)) {
+  double tot[3];
+  if (grid_reduce<3>(v, ws, tot)) {
     sc->true_r2 = tot[1];
     sc->lambda = tot[0];
     if (mode == 0) {
       sc->delta = tot[0];
       sc->beta = 0.0;
     } else {
-      sc->beta = tot[0] / sc->delta;
+      // no iteration yet (or a degenerate one): restart along r
+      sc->beta = (sc->iter > 0 && sc->pAp > 0.0) ? -tot[2] / sc->pAp : 0.0;
       sc->delta = tot[0];
       sc->n_rel += 1;
     }
@@ -229,7 +267,7 @@ struct GraphCache {
   int chunk = 0;
   MixScal* sc = nullptr;
   unsigned long long epoch = 0;
-  int doe_threads = 0;
+  int hop_shapes = -1;
 };
 GraphCache g_cache;
 cudaStream_t g_cap = nullptr;
@@ -253,49 +291,105 @@ void fp64_mdagm(const MixedBuffers& B, double2* out, const double2* in, double2*
   launch_dslash<double>(a);
 }
 
-// Block sizes the autotuner tries for k_mx_doe (the first is the default).
-static const int kDoeThreads[3] = {MX_THREADS, 256, 64};
+// Launch shapes the autotuner tries (the first is the default): block size
+// and hops in flight.  The block size of k_mx_deo_dot fixes the summation
+// order of <p, Ap>, so only its hops in flight are tuned.
+struct HopShape {
+  int threads, hb;
+};
+static const HopShape kDoeShapes[7] = {{MX_THREADS, 1}, {256, 1}, {64, 1}, {MX_THREADS, 2},
+                                       {MX_THREADS, 4}, {256, 2}, {64, 2}};
+static const HopShape kDeoShapes[3] = {{MX_THREADS, 1}, {MX_THREADS, 2}, {MX_THREADS, 4}};
 
-void launch_mx_doe(int threads, const MixedBuffers& B, const MixScal* sc, cudaStream_t st) {
+// Calls f with the view of the sloppy links the FP32 iteration reads.
+template <typename F>
+void with_sloppy_links(const MixedBuffers& B, F&& f) {
+  if (B.q16) f(B.uq);
+  else f(LinkView<float2>{B.u32, rt().g.sizeh, B.u32_compact ? 6 : 9});
+}
+
+template <int HB>
+void launch_mx_doe_t(int threads, const MixedBuffers& B, const MixScal* sc, cudaStream_t st) {
   const Geom& g = rt().g;
-  LinkView<float2> u{B.u32, g.sizeh, B.u32_compact ? 6 : 9};
   const int nb = blocks_for(g.sizeh, threads);
-  if (B.ph32_mode == PH_SIGN8) k_mx_doe<PH_SIGN8><<<nb, threads, 0, st>>>(g, u, B.ph32, B.p, B.t, sc);
-  else k_mx_doe<PH_ANGLE><<<nb, threads, 0, st>>>(g, u, B.ph32, B.p, B.t, sc);
+  with_sloppy_links(B, [&](const auto& u) {
+    typedef typename std::decay<decltype(u)>::type LV;
+    if (B.ph32_mode == PH_SIGN8) k_mx_doe<PH_SIGN8, LV, HB><<<nb, threads, 0, st>>>(g, u, B.ph32, B.p, B.t, sc);
+    else k_mx_doe<PH_ANGLE, LV, HB><<<nb, threads, 0, st>>>(g, u, B.ph32, B.p, B.t, sc);
+  });
 }
 
-int mx_doe_threads(const MixedBuffers& B) {
-  const int pick = autotune_cached(TUNE_MX_DOE, rt().g.sizeh, B.ph32_mode == PH_SIGN8);
-  return kDoeThreads[pick > 0 && pick < 3 ? pick : 0];
+void launch_mx_doe(HopShape sh, const MixedBuffers& B, const MixScal* sc, cudaStream_t st) {
+  if (sh.hb == 4) launch_mx_doe_t<4>(sh.threads, B, sc, st);
+  else if (sh.hb == 2) launch_mx_doe_t<2>(sh.threads, B, sc, st);
+  else launch_mx_doe_t<1>(sh.threads, B, sc, st);
 }
 
-// Tunes the k_mx_doe block size once per lattice (t is scratch; the timing
-// launches see a copy of the scalars with the solve running).
-int tune_mx_doe(const MixedBuffers& B, cudaStream_t st) {
-  const int variant = B.ph32_mode == PH_SIGN8;
-  if (autotune_cached(TUNE_MX_DOE, rt().g.sizeh, variant) < 0 && autotune_enabled()) {
+template <int HB>
+void launch_mx_deo_dot_t(const MixedBuffers& B, MixScal* sc, ReduceWs ws, cudaStream_t st) {
+  const Geom& g = rt().g;
+  const int nb = blocks_for(g.sizeh, MX_THREADS);
+  with_sloppy_links(B, [&](const auto& u) {
+    typedef typename std::decay<decltype(u)>::type LV;
+    if (B.ph32_mode == PH_SIGN8)
+      k_mx_deo_dot<PH_SIGN8, LV, HB><<<nb, MX_THREADS, 0, st>>>(g, u, B.ph32, B.t, B.p, B.s, sc, ws);
+    else k_mx_deo_dot<PH_ANGLE, LV, HB><<<nb, MX_THREADS, 0, st>>>(g, u, B.ph32, B.t, B.p, B.s, sc, ws);
+  });
+}
+
+void launch_mx_deo_dot(HopShape sh, const MixedBuffers& B, MixScal* sc, ReduceWs ws, cudaStream_t st) {
+  if (sh.hb == 4) launch_mx_deo_dot_t<4>(B, sc, ws, st);
+  else if (sh.hb == 2) launch_mx_deo_dot_t<2>(B, sc, ws, st);
+  else launch_mx_deo_dot_t<1>(B, sc, ws, st);
+}
+
+// blocks of the k_mx_deo_dot launch (the reductions' partial sums)
+int mx_deo_blocks() { return blocks_for(rt().g.sizeh, MX_THREADS); }
+
+int doe_variant(const MixedBuffers& B) { return (B.ph32_mode == PH_SIGN8) + 2 * (B.q16 != 0); }
+
+HopShape mx_doe_shape(const MixedBuffers& B) {
+  const int pick = autotune_cached(TUNE_MX_DOE, rt().g.sizeh, doe_variant(B));
+  return kDoeShapes[pick > 0 && pick < 7 ? pick : 0];
+}
+
+HopShape mx_deo_shape(const MixedBuffers& B) {
+  const int pick = autotune_cached(TUNE_MX_DEO, rt().g.sizeh, doe_variant(B));
+  return kDeoShapes[pick > 0 && pick < 3 ? pick : 0];
+}
+
+// Tunes the launch shapes of both hops once per lattice and link format
+// (t and s are scratch; the timing launches see a copy of the scalars with
+// the solve running and write their <p, Ap> into that copy).  Returns a key
+// of the chosen shapes for the graph cache.
+int tune_mx_hops(const MixedBuffers& B, cudaStream_t st) {
+  const int variant = doe_variant(B);
+  const long sh = rt().g.sizeh;
+  if (autotune_enabled() && (autotune_cached(TUNE_MX_DOE, sh, variant) < 0 ||
+                             autotune_cached(TUNE_MX_DEO, sh, variant) < 0)) {
     MixScal h;
     memset(&h, 0, sizeof(h));
-    const MixScal* sc = static_cast<const MixScal*>(autotune_scalars(&h, sizeof(h), st));
-    if (sc)
-      autotune_pick(TUNE_MX_DOE, rt().g.sizeh, variant, 3,
-                    [&](int c) { launch_mx_doe(kDoeThreads[c], B, sc, st); }, st);
+    h.delta = 1.0;
+    MixScal* sc = static_cast<MixScal*>(autotune_scalars(&h, sizeof(h), st));
+    if (sc) {
+      autotune_pick(TUNE_MX_DOE, sh, variant, 7, [&](int c) { launch_mx_doe(kDoeShapes[c], B, sc, st); }, st);
+      ReduceWs ws = reduce_ws(1, mx_deo_blocks());
+      autotune_pick(TUNE_MX_DEO, sh, variant, 3, [&](int c) { launch_mx_deo_dot(kDeoShapes[c], B, sc, ws, st); },
+                    st);
+    }
   }
-  return mx_doe_threads(B);
+  const int a = autotune_cached(TUNE_MX_DOE, sh, variant), b = autotune_cached(TUNE_MX_DEO, sh, variant);
+  return (a < 0 ? 0 : a) * 16 + (b < 0 ? 0 : b);
 }
 
 void enqueue_iteration(const MixedBuffers& B, MixScal* sc, cudaStream_t st) {
   const Geom& g = rt().g;
-  LinkView<float2> u{B.u32, g.sizeh, B.u32_compact ? 6 : 9};
-  const int nb = blocks_for(g.sizeh, MX_THREADS);
   const long n4 = 3L * g.sizeh / 2;
   int gr = reduce_grid(n4);
-  int gd = nb;
+  int gd = mx_deo_blocks();
   ReduceWs wsd = reduce_ws(1, gd > gr ? gd : gr);
-  launch_mx_doe(mx_doe_threads(B), B, sc, st);
-  if (B.ph32_mode == PH_SIGN8)
-    k_mx_deo_dot<PH_SIGN8><<<nb, MX_THREADS, 0, st>>>(g, u, B.ph32, B.t, B.p, B.s, sc, wsd);
-  else k_mx_deo_dot<PH_ANGLE><<<nb, MX_THREADS, 0, st>>>(g, u, B.ph32, B.t, B.p, B.s, sc, wsd);
+  launch_mx_doe(mx_doe_shape(B), B, sc, st);
+  launch_mx_deo_dot(mx_deo_shape(B), B, sc, wsd, st);
   g_kernel_launches += 2;
   k_mx_update<<<gr, RED_THREADS, 0, st>>>(reinterpret_cast<float4*>(B.xf), reinterpret_cast<float4*>(B.r),
                                           reinterpret_cast<const float4*>(B.p),
@@ -355,21 +449,21 @@ MixedResult mixed_cg(const MixedBuffers& B, const MixedOptions& o, MixScal* sc, 
   else fp64_mdagm(B, B.t64, B.x, B.t64b, o.mass2, cs);
   {
     int gr = reduce_grid(n);
-    k_mx_residual<<<gr, RED_THREADS, 0, cs>>>(B.b, B.t64, B.r64, B.r, B.p, n, sc, reduce_ws(2, gr), 0);
+    k_mx_residual<<<gr, RED_THREADS, 0, cs>>>(B.b, B.t64, B.r64, B.r, B.p, B.s, n, sc, reduce_ws(3, gr), 0);
     OST_LAUNCH_CHECK();
   }
 
   // workspace used inside the captured chunk is allocated before capture
   {
-    const int nb = blocks_for(g.sizeh, MX_THREADS);
+    const int nb = mx_deo_blocks();
     const int gr = reduce_grid(n);
-    reduce_ws(2, nb > gr ? nb : gr);
+    reduce_ws(3, nb > gr ? nb : gr);   // the reliable updates' k_mx_residual sums 3 values
   }
   // launch shape of the D_oe (numerics-invariant), chosen before the capture
-  const int doe_threads = tune_mx_doe(B, cs);
+  const int hop_shapes = tune_mx_hops(B, cs);
   // (re)capture the iteration chunk
   if (!g_cache.exec || !same_key(g_cache.key, B) || g_cache.chunk != o.chunk || g_cache.sc != sc ||
-      g_cache.epoch != runtime_epoch() || g_cache.doe_threads != doe_threads) {
+      g_cache.epoch != runtime_epoch() || g_cache.hop_shapes != hop_shapes) {
     if (g_cache.exec) cudaGraphExecDestroy(g_cache.exec);
     g_cache.exec = nullptr;
     cudaGraph_t graph;
@@ -384,7 +478,7 @@ MixedResult mixed_cg(const MixedBuffers& B, const MixedOptions& o, MixScal* sc, 
     g_cache.chunk = o.chunk;
     g_cache.sc = sc;
     g_cache.epoch = runtime_epoch();
-    g_cache.doe_threads = doe_threads;
+    g_cache.hop_shapes = hop_shapes;
   }
 
   const long n4 = n / 2;
@@ -404,7 +498,7 @@ MixedResult mixed_cg(const MixedBuffers& B, const MixedOptions& o, MixScal* sc, 
       if (B.use_df) df_mdagm(B.df, B.dfw, B.t64, B.x, o.mass2, cs);
       else fp64_mdagm(B, B.t64, B.x, B.t64b, o.mass2, cs);
       int gr = reduce_grid(n);
-      k_mx_residual<<<gr, RED_THREADS, 0, cs>>>(B.b, B.t64, B.r64, B.r, B.p, n, sc, reduce_ws(2, gr), 1);
+      k_mx_residual<<<gr, RED_THREADS, 0, cs>>>(B.b, B.t64, B.r64, B.r, B.p, B.s, n, sc, reduce_ws(3, gr), 1);
       OST_LAUNCH_CHECK();
       k_mx_pupdate<<<reduce_grid(n4), RED_THREADS, 0, cs>>>(reinterpret_cast<float4*>(B.p),
                                                             reinterpret_cast<const float4*>(B.r), n4, sc, 0);
@@ -418,7 +512,7 @@ MixedResult mixed_cg(const MixedBuffers& B, const MixedOptions& o, MixScal* sc, 
       fp64_mdagm(B, B.t64, B.x, B.t64b, o.mass2, cs);
       int gr = reduce_grid(n);
       // mode 1 recomputes r, resets last_max and re-evaluates done
-      k_mx_residual<<<gr, RED_THREADS, 0, cs>>>(B.b, B.t64, B.r64, B.r, B.p, n, sc, reduce_ws(2, gr), 1);
+      k_mx_residual<<<gr, RED_THREADS, 0, cs>>>(B.b, B.t64, B.r64, B.r, B.p, B.s, n, sc, reduce_ws(3, gr), 1);
       OST_LAUNCH_CHECK();
       OST_CUDA(cudaMemcpyAsync(g_host, sc, sizeof(MixScal), cudaMemcpyDeviceToHost, cs));
       OST_CUDA(cudaStreamSynchronize(cs));
@@ -447,20 +541,40 @@ MixedResult mixed_cg(const MixedBuffers& B, const MixedOptions& o, MixScal* sc, 
   return res;
 }
 
+// out = m2 in - D_eo D_oe in through the FP32 iteration kernels (the sloppy
+// operator of the solve, with B's link format), FP64 in and out.  Uses B.p,
+// B.t and B.s as work and sc as scratch scalars.
+void sloppy_mdagm(const MixedBuffers& B, double m2, const double2* in, double2* out, MixScal* sc, cudaStream_t st) {
+  const long n = 3L * rt().g.sizeh;
+  MixScal init;
+  memset(&init, 0, sizeof(init));
+  init.m2 = m2;
+  init.delta = 1.0;
+  OST_CUDA(cudaMemcpyAsync(sc, &init, sizeof(MixScal), cudaMemcpyHostToDevice, st));
+  ReduceWs ws = reduce_ws(1, mx_deo_blocks());
+  conv_d2f(in, B.p, n, st);
+  launch_mx_doe(kDoeShapes[0], B, sc, st);
+  launch_mx_deo_dot(kDeoShapes[0], B, sc, ws, st);
+  OST_LAUNCH_CHECK();
+  conv_f2d(B.s, out, n, st);
+  OST_CUDA(cudaStreamSynchronize(st));
+}
+
 // Times `reps` launches of one FP32 solver kernel on stream st with CUDA
 // events recorded on that stream; returns the mean milliseconds per launch.
 // which = 1: D_oe (t = D_oe p); which = 2: fused D_eo + M^+M epilogue + dot.
 double time_mixed_kernel(const MixedBuffers& B, MixScal* sc, int which, int reps, cudaStream_t st) {
   const Geom& g = rt().g;
-  LinkView<float2> u{B.u32, g.sizeh, B.u32_compact ? 6 : 9};
-  const int nb = blocks_for(g.sizeh, MX_THREADS);
+  const int nb = mx_deo_blocks();
   MixScal init;
   memset(&init, 0, sizeof(init));
   init.m2 = 0.01;
   init.delta = 1.0;
   OST_CUDA(cudaMemcpyAsync(sc, &init, sizeof(MixScal), cudaMemcpyHostToDevice, st));
   ReduceWs ws = reduce_ws(1, nb);
-  const int doe_threads = which == 1 ? tune_mx_doe(B, st) : MX_THREADS;
+  tune_mx_hops(B, st);
+  const HopShape doe_shape = mx_doe_shape(B);
+  const HopShape deo_shape = mx_deo_shape(B);
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
@@ -469,11 +583,9 @@ double time_mixed_kernel(const MixedBuffers& B, MixScal* sc, int which, int reps
     cudaEventRecord(e0, st);
     for (int k = 0; k < reps; ++k) {
       if (which == 1) {
-        launch_mx_doe(doe_threads, B, sc, st);
+        launch_mx_doe(doe_shape, B, sc, st);
       } else {
-        if (B.ph32_mode == PH_SIGN8)
-          k_mx_deo_dot<PH_SIGN8><<<nb, MX_THREADS, 0, st>>>(g, u, B.ph32, B.t, B.p, B.s, sc, ws);
-        else k_mx_deo_dot<PH_ANGLE><<<nb, MX_THREADS, 0, st>>>(g, u, B.ph32, B.t, B.p, B.s, sc, ws);
+        launch_mx_deo_dot(deo_shape, B, sc, ws, st);
       }
       OST_LAUNCH_CHECK();
     }

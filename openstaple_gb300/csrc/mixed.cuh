@@ -1,5 +1,6 @@
 // mixed.cuh -- single-precision solver engine with FP64 reliable updates.
 #pragma once
+#include "dslash.cuh"
 #include <cuda_runtime.h>
 #include "common.cuh"
 #include "dslash_df.cuh"
@@ -52,6 +53,8 @@ struct MixedBuffers {
   const void* ph64;        // double angles [8][sizeh]
   const float2* u32;       // single-precision links
   int u32_compact;         // 1: two rows per direction
+  int q16;                 // 1: the FP32 iteration reads the 16-bit links uq instead of u32
+  LinkQ16 uq;
   const void* ph32;        // sign bytes or float angles
   int ph32_mode;           // PhaseMode for the FP32 kernels
   double2* x;              // solution (in: guess, out: result)
@@ -71,6 +74,9 @@ struct MixedBuffers {
 
 // Converts the first two rows of FP64 su3_soa[8] links to a compact FP32 copy.
 void links_to_f32_compact(const double2* u64, float2* u32, long sizeh, cudaStream_t st);
+// Converts the first two rows of FP64 su3_soa[8] links to the 16-bit
+// fixed-point planes of LinkQ16 (a: 8 x sizeh uint4, b: 8 x sizeh uint2).
+void links_to_q16(const double2* u64, uint4* a, uint2* b, long sizeh, cudaStream_t st);
 // Sign bytes from FP64 phase angles; *all_exact (device int) is cleared when
 // some angle is neither 0 nor pi.
 void phases_to_signs(const double* ph64, unsigned char* sg, int* all_exact, long sizeh, cudaStream_t st);
@@ -80,5 +86,12 @@ void phases_to_f32(const double* ph64, float* ph32, long sizeh, cudaStream_t st)
 MixedResult mixed_cg(const MixedBuffers& B, const MixedOptions& o, MixScal* scal_dev, cudaStream_t st);
 
 double time_mixed_kernel(const MixedBuffers& B, MixScal* sc, int which, int reps, cudaStream_t st);
+
+// out = m2 in - D_eo D_oe in with the FP32 iteration kernels and B's links.
+void sloppy_mdagm(const MixedBuffers& B, double m2, const double2* in, double2* out, MixScal* sc, cudaStream_t st);
+
+// Link format of the FP32 iteration when the library converts the links
+// itself: 1 (default) 16-bit fixed point (LinkQ16), 0 two FP32 rows.
+int sloppy_links_q16();
 
 }  // namespace ost

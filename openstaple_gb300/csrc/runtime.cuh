@@ -78,6 +78,7 @@ enum WorkspaceSlot {
   WS_BATCH64,
   WS_LINKS_LO,     // lo parts of the double-float links
   WS_DF,           // double-float M^+M work fields
+  WS_LINKS_Q16,    // 16-bit fixed-point sloppy links
   WS_NSLOTS
 };
 

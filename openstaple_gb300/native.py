@@ -114,6 +114,8 @@ SIGNATURES = {
     "real_scal_prod_global": (_D, [_P, _P]),
     "l2norm2_global": (_D, [_P]),
     "ostaple_mdagm_df": (_I, [_P, _P, _D, _D, _P, _P]),
+    "ostaple_set_sloppy_links": (_I, [_I]),
+    "ostaple_mdagm_sloppy": (_I, [_P, _P, _D, _D, _P, _P]),
     "ostaple_net_weights_save": (_I, [C.c_char_p, _P]),
     "ostaple_net_weights_load": (_I, [C.c_char_p, _P]),
     "ostaple_selftest_bounded_wait": (_I, [_I]),

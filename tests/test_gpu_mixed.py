@@ -105,3 +105,74 @@ def test_mixed_with_generic_phases(lat_factory):
     lat.update_host(x)
     assert info["status"] == 1
     assert true_residual(o, u, ph, 0.05, x, b, 0.1) <= 1e-10
+
+
+def quantize_links_q16(u):
+    """The 16-bit fixed-point sloppy links as the FP32 kernels see them: the
+    first two rows rounded to multiples of 2^-15 (half to even, clamped to
+    +-32767/32768), the third row rebuilt as conj(row0 x row1)."""
+    q = np.clip(np.rint(u.real * 32768.0), -32767, 32767) + 1j * np.clip(np.rint(u.imag * 32768.0), -32767, 32767)
+    q = q / 32768.0
+    a, c = q[:, 0], q[:, 1]
+    q[:, 2] = np.conj(np.stack([a[:, 1] * c[:, 2] - a[:, 2] * c[:, 1],
+                                a[:, 2] * c[:, 0] - a[:, 0] * c[:, 2],
+                                a[:, 0] * c[:, 1] - a[:, 1] * c[:, 0]], axis=1))
+    return np.ascontiguousarray(q)
+
+
+@pytest.mark.parametrize("fmt", ["f32", "q16"])
+@pytest.mark.parametrize("im_chem_pot", [0.0, 0.2])
+def test_sloppy_operator(lat_factory, fmt, im_chem_pot):
+    """The FP32 iteration's M^+M with each sloppy link format: against the
+    FP64 oracle on the links the kernels see (FP32 arithmetic, 2e-6), and for
+    the 16-bit links against the exact links (quantisation, 1e-4)."""
+    from oracle import Oracle
+    dims = (8, 4, 6, 8)
+    o = Oracle(dims)
+    lat = lat_factory(dims)
+    u = F.random_su3_links(dims, 91)
+    ph = F.staggered_phases(dims, im_chem_pot=im_chem_pot)
+    b = F.gaussian_vec3(dims, 92)
+    out = lat.vec3()
+    for a in (u, ph, b, out):
+        lat.present(a)
+    prev = api.set_sloppy_links(fmt)
+    try:
+        api.mdagm_sloppy(u, ph, 0.03, out, b, shift=0.01)
+    finally:
+        api.set_sloppy_links(prev)
+    lat.update_host(out)
+    m2 = 0.03 ** 2 + 0.01
+    seen = quantize_links_q16(u) if fmt == "q16" else u
+    assert relerr(out, o.mdagm(seen, b, ph, m2)) <= 2e-6
+    if fmt == "q16":
+        assert relerr(out, o.mdagm(u, b, ph, m2)) <= 1e-4
+
+
+def test_q16_links_converge_like_f32(lat_factory):
+    """Both sloppy link formats reach the FP64 target; the 16-bit links cost
+    at most a few per cent more iterations."""
+    from oracle import Oracle
+    dims = (16, 8, 8, 8)
+    o = Oracle(dims)
+    lat = lat_factory(dims)
+    u = F.random_su3_links(dims, 93)
+    b = F.gaussian_vec3(dims, 94)
+    ph = F.staggered_phases(dims)
+    x = lat.vec3()
+    for a in (u, b, ph, x):
+        lat.present(a)
+    iters = {}
+    for fmt in ("f32", "q16"):
+        prev = api.set_sloppy_links(fmt)
+        try:
+            x[:] = 0
+            lat.update_device(x)
+            info = api.invert_mixed(u, ph, 0.01, 0.0, x, b, 1e-10, 20000, 0, 1e-4)
+        finally:
+            api.set_sloppy_links(prev)
+        lat.update_host(x)
+        assert info["status"] == 1, (fmt, info)
+        assert true_residual(o, u, ph, 0.01, x, b) <= 1e-10
+        iters[fmt] = info["iters"]
+    assert iters["q16"] <= 1.1 * iters["f32"] + 5, iters
