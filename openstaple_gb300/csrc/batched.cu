@@ -8,6 +8,7 @@
 // are captured as CUDA graphs and polled once per chunk.
 #include <cmath>
 #include <cstring>
+#include <type_traits>
 #include "autotune.cuh"
 #include "batched.cuh"
 #include "dslash.cuh"
@@ -54,9 +55,9 @@ OST_D unsigned active_mask(const BatchScal* sc) {
 // fields start at in + sys[j] * vs.  All loads of one hop are issued before
 // its arithmetic; the link, its sign and its rebuilt third row serve all SPL
 // systems.
-template <int SPL, int P, int PH>
-OST_D void hop_multi(const Geom& g, const LinkView<float2>& u, const float2* in, long vs, const int sys[SPL],
-                     const void* phases, int idx, float2 aux[SPL][3]) {
+template <int SPL, int P, int PH, typename LV>
+OST_D void hop_multi(const Geom& g, const LV& u, const float2* in, long vs, const int sys[SPL], const void* phases,
+                     int idx, float2 aux[SPL][3]) {
   const long sh = g.sizeh;
   Site st = site_of(g, idx, P);
   int fwd[4], bwd[4];
@@ -137,10 +138,10 @@ OST_D bool hop_thread(long sizeh, int& idx, int sys[HopLayout<NS, SPL_>::SPL], b
 
 // t_k = D_oe p_k (every system of the batch; converged ones are recomputed
 // harmlessly since t is a temporary)
-template <int NS, int SPL_, int PH>
+template <int NS, int SPL_, int PH, typename LV>
 __global__ void __launch_bounds__(BT)
-k_b_doe(Geom g, LinkView<float2> u, const void* __restrict__ ph, const float2* __restrict__ p, float2* __restrict__ t,
-        long vs, const BatchScal* sc) {
+k_b_doe(Geom g, LV u, const void* __restrict__ ph, const float2* __restrict__ p, float2* __restrict__ t, long vs,
+        const BatchScal* sc) {
   typedef HopLayout<NS, SPL_> H;
   if (!active_mask(sc)) return;
   int idx, sys[H::SPL];
@@ -191,10 +192,10 @@ OST_D bool hop_reduce(const float v[HopLayout<NS>::SPL], ReduceWs ws, double tot
 }
 
 // s_k = m2_k p_k - D_eo t_k ; pAp_k ; alpha_k = delta_k / pAp_k
-template <int NS, int PH>
+template <int NS, int PH, typename LV>
 __global__ void __launch_bounds__(BT)
-k_b_deo_dot(Geom g, LinkView<float2> u, const void* __restrict__ ph, const float2* __restrict__ t,
-            const float2* __restrict__ p, float2* __restrict__ s, long vs, BatchScal* sc, ReduceWs ws) {
+k_b_deo_dot(Geom g, LV u, const void* __restrict__ ph, const float2* __restrict__ t, const float2* __restrict__ p,
+            float2* __restrict__ s, long vs, BatchScal* sc, ReduceWs ws) {
   typedef HopLayout<NS> H;
   if (!active_mask(sc)) return;
   int idx, sys[H::SPL];
@@ -342,29 +343,37 @@ __global__ void k_b_accumulate(double2* __restrict__ x, float2* __restrict__ xf,
 }
 
 // r64 = b - Ax, r = (float) r64 for system k; mode 0 initial, mode 1 reliable update
+// (mode 1: beta = -<r, s>/<p, s> with s = A p of system k's last iteration,
+// the Hestenes-Stiefel form the single-system solver uses at its reliable
+// updates, k_mx_residual)
 __global__ void k_b_residual(const double2* __restrict__ b, const double2* __restrict__ ax, double2* __restrict__ r64,
-                             float2* __restrict__ r, float2* __restrict__ p, long n, BatchScal* sc, int k,
-                             ReduceWs ws, int mode) {
-  double v[2] = {0.0, 0.0};
+                             float2* __restrict__ r, float2* __restrict__ p, const float2* __restrict__ s, long n,
+                             BatchScal* sc, int k, ReduceWs ws, int mode) {
+  double v[3] = {0.0, 0.0, 0.0};
   for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n; i += long(gridDim.x) * blockDim.x) {
     double2 bb = b[i], a = ax[i];
     double2 d = make_double2(bb.x - a.x, bb.y - a.y);
     r64[i] = d;
     float2 f = make_float2(float(d.x), float(d.y));
     r[i] = f;
-    if (mode == 0) p[i] = f;
+    if (mode == 0) {
+      p[i] = f;
+    } else {
+      const float2 sv = s[i];
+      v[2] += double(f.x) * sv.x + double(f.y) * sv.y;
+    }
     v[0] += double(f.x) * f.x + double(f.y) * f.y;
     v[1] += d.x * d.x + d.y * d.y;
   }
-  double tot[2];
-  if (grid_reduce<2>(v, ws, tot)) {
+  double tot[3];
+  if (grid_reduce<3>(v, ws, tot)) {
     sc->true_r2[k] = tot[1];
     sc->lambda[k] = tot[0];
     if (mode == 0) {
       sc->delta[k] = tot[0];
       sc->beta[k] = 0.0;
     } else {
-      sc->beta[k] = tot[0] / sc->delta[k];
+      sc->beta[k] = (sc->iter[k] > 0 && sc->pAp[k] > 0.0) ? -tot[2] / sc->pAp[k] : 0.0;
       sc->delta[k] = tot[0];
       sc->n_rel[k] += 1;
     }
@@ -379,15 +388,30 @@ __global__ void k_b_residual(const double2* __restrict__ b, const double2* __res
 // so the results are the same for every choice).
 static const int kSplCand[4] = {0, 1, 2, 4};
 
+// Calls f with the view of the sloppy links of the batched iteration.
+template <typename F>
+void with_batch_links(const BatchBuffers& B, F&& f) {
+  if (B.q16) f(B.uq);
+  else f(LinkView<float2>{B.u32, rt().g.sizeh, 6});
+}
+
 template <int NS, int SPL_>
 void launch_b_doe_spl(const BatchBuffers& B, BatchScal* sc, cudaStream_t st) {
   const Geom& g = rt().g;
-  LinkView<float2> u{B.u32, g.sizeh, 6};
   const long n = 3L * g.sizeh;
   const int nb = hop_blocks<NS, SPL_>(g.sizeh);
-  if (B.ph32_mode == PH_SIGN8) k_b_doe<NS, SPL_, PH_SIGN8><<<nb, BT, 0, st>>>(g, u, B.ph32, B.p, B.t, n, sc);
-  else k_b_doe<NS, SPL_, PH_ANGLE><<<nb, BT, 0, st>>>(g, u, B.ph32, B.p, B.t, n, sc);
+  with_batch_links(B, [&](const auto& u) {
+    typedef typename std::decay<decltype(u)>::type LV;
+    if (B.ph32_mode == PH_SIGN8) k_b_doe<NS, SPL_, PH_SIGN8, LV><<<nb, BT, 0, st>>>(g, u, B.ph32, B.p, B.t, n, sc);
+    else k_b_doe<NS, SPL_, PH_ANGLE, LV><<<nb, BT, 0, st>>>(g, u, B.ph32, B.p, B.t, n, sc);
+  });
   OST_LAUNCH_CHECK();
+}
+
+// tuning key of k_b_doe: systems, phase mode, link format
+template <int NS>
+int b_doe_variant(const BatchBuffers& B) {
+  return NS * 4 + (B.ph32_mode == PH_SIGN8) * 2 + (B.q16 != 0);
 }
 
 template <int NS>
@@ -425,17 +449,20 @@ void fp64_mdagm(const BatchBuffers& B, double2* out, const double2* in, double m
 template <int NS>
 void enqueue_batch_iteration(const BatchBuffers& B, BatchScal* sc, cudaStream_t st) {
   const Geom& g = rt().g;
-  LinkView<float2> u{B.u32, g.sizeh, 6};
   const int nb = hop_blocks<NS>(g.sizeh);
   const long n = 3L * g.sizeh, n4 = n / 2;
   const int bps = seg_blocks(n4, NS);
   // one workspace for both reductions: hop (SLOTS x nb partials) and
   // segments (NS x bps partials)
   ReduceWs wh = reduce_ws(HopLayout<NS>::SLOTS, nb > NS * bps ? nb : NS * bps);
-  const int pick = autotune_cached(TUNE_B_DOE, g.sizeh, NS * 2 + (B.ph32_mode == PH_SIGN8));
+  const int pick = autotune_cached(TUNE_B_DOE, g.sizeh, b_doe_variant<NS>(B));
   launch_b_doe<NS>(kSplCand[pick > 0 && pick < 4 ? pick : 0], B, sc, st);
-  if (B.ph32_mode == PH_SIGN8) k_b_deo_dot<NS, PH_SIGN8><<<nb, BT, 0, st>>>(g, u, B.ph32, B.t, B.p, B.s, n, sc, wh);
-  else k_b_deo_dot<NS, PH_ANGLE><<<nb, BT, 0, st>>>(g, u, B.ph32, B.t, B.p, B.s, n, sc, wh);
+  with_batch_links(B, [&](const auto& u) {
+    typedef typename std::decay<decltype(u)>::type LV;
+    if (B.ph32_mode == PH_SIGN8)
+      k_b_deo_dot<NS, PH_SIGN8, LV><<<nb, BT, 0, st>>>(g, u, B.ph32, B.t, B.p, B.s, n, sc, wh);
+    else k_b_deo_dot<NS, PH_ANGLE, LV><<<nb, BT, 0, st>>>(g, u, B.ph32, B.t, B.p, B.s, n, sc, wh);
+  });
   k_b_update<NS><<<NS * bps, RED_THREADS, 0, st>>>(reinterpret_cast<float4*>(B.xf), reinterpret_cast<float4*>(B.r),
                                                     reinterpret_cast<const float4*>(B.p),
                                                     reinterpret_cast<const float4*>(B.s), n4, n4, bps, sc, wh);
@@ -456,7 +483,7 @@ inline size_t batch_reduce_partials(long sizeh) {
 
 template <int NS>
 int tune_b_doe(const BatchBuffers& B, cudaStream_t st) {
-  const int variant = NS * 2 + (B.ph32_mode == PH_SIGN8);
+  const int variant = b_doe_variant<NS>(B);
   const int cached = autotune_cached(TUNE_B_DOE, rt().g.sizeh, variant);
   if (cached >= 0 || !autotune_enabled()) return cached > 0 ? cached : 0;
   BatchScal h;
@@ -558,8 +585,8 @@ BatchResult batched_mixed_cg(const BatchBuffers& B, const double* m2, double res
     else if (B.use_df) df_mdagm(B.df, B.dfw, B.t64, B.x + k * n, m2[k], cs);
     else fp64_mdagm(B, B.t64, B.x + k * n, m2[k], cs);
     const int gr = reduce_grid(n);
-    k_b_residual<<<gr, RED_THREADS, 0, cs>>>(B.b + k * n, B.t64, B.r64, B.r + k * n, B.p + k * n, n, sc, k,
-                                             reduce_ws(2, gr), 0);
+    k_b_residual<<<gr, RED_THREADS, 0, cs>>>(B.b + k * n, B.t64, B.r64, B.r + k * n, B.p + k * n, B.s + k * n, n, sc, k,
+                                             reduce_ws(3, gr), 0);
     OST_LAUNCH_CHECK();
   }
   bool finished[BATCH_MAX] = {false};
@@ -577,6 +604,7 @@ BatchResult batched_mixed_cg(const BatchBuffers& B, const double* m2, double res
       g_bgraph.doe_pick != doe_pick ||
       g_bgraph.key.p != B.p || g_bgraph.key.r != B.r || g_bgraph.key.s != B.s || g_bgraph.key.t != B.t ||
       g_bgraph.key.xf != B.xf || g_bgraph.key.u32 != B.u32 || g_bgraph.key.ph32 != B.ph32 ||
+      g_bgraph.key.q16 != B.q16 || g_bgraph.key.uq.a != B.uq.a ||
       g_bgraph.key.ph32_mode != B.ph32_mode || g_bgraph.epoch != runtime_epoch()) {
     if (g_bgraph.exec) cudaGraphExecDestroy(g_bgraph.exec);
     cudaGraph_t graph;
@@ -609,8 +637,8 @@ BatchResult batched_mixed_cg(const BatchBuffers& B, const double* m2, double res
         if (!was_done && B.use_df) df_mdagm(B.df, B.dfw, B.t64, B.x + k * n, m2[k], cs);
         else fp64_mdagm(B, B.t64, B.x + k * n, m2[k], cs);
         const int gr = reduce_grid(n);
-        k_b_residual<<<gr, RED_THREADS, 0, cs>>>(B.b + k * n, B.t64, B.r64, B.r + k * n, B.p + k * n, n, sc, k,
-                                                 reduce_ws(2, gr), 1);
+        k_b_residual<<<gr, RED_THREADS, 0, cs>>>(B.b + k * n, B.t64, B.r64, B.r + k * n, B.p + k * n, B.s + k * n, n, sc, k,
+                                                 reduce_ws(3, gr), 1);
         OST_LAUNCH_CHECK();
         if (was_done) {
           OST_CUDA(cudaMemcpyAsync(g_bhost, sc, sizeof(BatchScal), cudaMemcpyDeviceToHost, cs));

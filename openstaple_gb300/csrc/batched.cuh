@@ -25,6 +25,8 @@ struct BatchBuffers {
   const double2* u64;       // reference su3_soa[8]
   const void* ph64;         // double angles
   const float2* u32;        // compact FP32 links
+  int q16;                  // 1: the FP32 iteration reads the 16-bit links uq instead of u32
+  LinkQ16 uq;
   const void* ph32;         // sign bytes or float angles
   int ph32_mode;
   int nsys;

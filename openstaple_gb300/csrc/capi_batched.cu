@@ -20,6 +20,8 @@ struct Prepared {
   const float2* u32;
   const void* ph;
   int mode;
+  int q16;        // 16-bit links for the batched FP32 iteration (the CG-M phase keeps u32)
+  LinkQ16 uq;
 };
 
 bool prepare(const Z* u64, const double* ph64, Prepared* out, cudaStream_t st) {
@@ -28,6 +30,17 @@ bool prepare(const Z* u64, const double* ph64, Prepared* out, cudaStream_t st) {
   char* sg = static_cast<char*>(workspace(WS_SIGNS, 256 + 8 * size_t(sh) * sizeof(float)));
   if (!u32 || !sg) return false;
   links_to_f32_compact(u64, u32, sh, st);
+  out->q16 = 0;
+  out->uq = LinkQ16{nullptr, nullptr, sh};
+  if (sloppy_links_q16()) {
+    char* q = static_cast<char*>(workspace(WS_LINKS_Q16, 8 * 24 * size_t(sh)));
+    if (!q) return false;
+    uint4* a = reinterpret_cast<uint4*>(q);
+    uint2* b = reinterpret_cast<uint2*>(q + 8 * 16 * size_t(sh));
+    links_to_q16(u64, a, b, sh, st);
+    out->q16 = 1;
+    out->uq = LinkQ16{a, b, sh};
+  }
   int* flag = reinterpret_cast<int*>(sg);
   const int one = 1;
   OST_CUDA(cudaMemcpyAsync(flag, &one, sizeof(int), cudaMemcpyHostToDevice, st));
@@ -105,6 +118,7 @@ int ostaple_invert_mixed_batch(const su3_soa* u, const double_soa* phases, doubl
     BatchBuffers B{};
     if (!batch_buffers(m, &B)) return INVERTER_FAILURE;
     B.u64 = u64; B.ph64 = ph; B.u32 = pr.u32; B.ph32 = pr.ph; B.ph32_mode = pr.mode;
+    B.q16 = pr.q16; B.uq = pr.uq;
     B.use_df = use_df;
     B.df = dop;
     B.dfw = dwk;
@@ -198,6 +212,7 @@ int ostaple_multishift_batch(const su3_soa* u, const double_soa* phases, double 
     BatchBuffers B{};
     if (!batch_buffers(m, &B)) return INVERTER_FAILURE;
     B.u64 = u64; B.ph64 = ph; B.u32 = pr.u32; B.ph32 = pr.ph; B.ph32_mode = pr.mode;
+    B.q16 = pr.q16; B.uq = pr.uq;
     B.use_df = use_df;
     B.df = dop;
     B.dfw = dwk;

@@ -98,3 +98,28 @@ def test_multishift_batch(lat_factory, nrhs):
             assert info["true_res"][r, k] <= 1e-10
             assert true_residual(o, u, ph, 0.05, xs[r, k], b[r], shifts[k]) <= 1e-10
             assert relerr(xs[r, k], xo[k]) <= 1e-8
+
+
+@pytest.mark.parametrize("fmt", ["f32", "q16"])
+def test_mixed_batch_link_formats(lat_factory, fmt):
+    """Both sloppy link formats of the batched FP32 iteration reach every
+    system's FP64 target at a light mass."""
+    from oracle import Oracle
+    dims = (8, 8, 8, 8)
+    o = Oracle(dims)
+    lat = lat_factory(dims)
+    u = F.random_su3_links(dims, 361)
+    ph = F.staggered_phases(dims)
+    b = np.stack([F.gaussian_vec3(dims, 370 + k) for k in range(4)])
+    x = lat.vec3(4)
+    for a in (u, ph, b, x):
+        lat.present(a)
+    prev = api.set_sloppy_links(fmt)
+    try:
+        info = api.invert_mixed_batch(u, ph, 0.01, x, b, None, 1e-10, 100000, 1e-4)
+    finally:
+        api.set_sloppy_links(prev)
+    lat.update_host(x)
+    assert info["status"] == 1, info
+    for k in range(4):
+        assert true_residual(o, u, ph, 0.01, x[k], b[k]) <= 1e-10
