@@ -94,6 +94,12 @@ template <typename T> struct cplx_t;
 template <> struct cplx_t<double> { typedef double2 type; };
 template <> struct cplx_t<float> { typedef float2 type; };
 
+// Device side of a programmatic dependent launch (launch_pdl): wait until
+// the previous kernel on the stream has completed and its writes are
+// visible; allow the next kernel to be scheduled.
+OST_D void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+OST_D void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 template <typename C> OST_HD C cmk(decltype(C().x) r, decltype(C().x) i) { C z; z.x = r; z.y = i; return z; }
 
 // a*b and a*conj(b), conj(a)*b with explicit FMA contraction order.

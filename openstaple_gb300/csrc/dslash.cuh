@@ -10,6 +10,7 @@
 // The reference subtracts the four backward terms first, then adds the four
 // forward terms; the same order is kept here.
 #pragma once
+#include <type_traits>
 #include "common.cuh"
 
 namespace ost {
@@ -368,6 +369,32 @@ OST_D void hop4(const LV& u, const float2* in, const void* phases, long sh, int 
       float2 m[6];
       raw[k].rows(m);
       mac_hop(acc, m, v[k], back);
+    }
+  }
+}
+
+OST_D void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+
+// L2 prefetches of the eight links the hop term of site idx (parity P) reads
+// (no data returns to the thread)
+template <int P, typename LV>
+OST_D void prefetch_links(const Geom& g, const LV& u, int idx) {
+  const long sh = g.sizeh;
+  Site s = site_of(g, idx, P);
+  int fwd[4], bwd[4];
+  neighbours(g, s, fwd, bwd);
+#pragma unroll
+  for (int hm = 0; hm < 8; ++hm) {
+    const bool back = hm < 4;
+    const int mu = hm & 3;
+    const int dir = back ? 2 * mu + (1 - P) : 2 * mu + P;
+    const int l = back ? bwd[mu] : idx;
+    if constexpr (std::is_same<LV, LinkQ16>::value) {
+      prefetch_l2(u.a + long(dir) * sh + l);
+      prefetch_l2(u.b + long(dir) * sh + l);
+    } else {
+#pragma unroll
+      for (int e = 0; e < 6; ++e) prefetch_l2(u.at(dir, e / 3, e % 3) + l);
     }
   }
 }

@@ -94,8 +94,13 @@ template <int PH, typename LV, int HB>
 __global__ void __launch_bounds__(256)
 k_mx_doe(Geom g, LV u, const void* __restrict__ ph, const float2* __restrict__ p, float2* __restrict__ t,
          const MixScal* sc) {
-  if (halted(sc)) return;
+  if (halted(sc)) return;   // set by k_mx_update, two launches back
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  // launched early (programmatic dependent launch): fetch the links, which
+  // no kernel of the solve writes, while the previous kernel finishes
+  if (idx < g.sizeh) prefetch_links<1>(g, u, idx);
+  pdl_wait();               // p from k_mx_pupdate
+  pdl_trigger();
   if (idx >= g.sizeh) return;
   float2 aux[3];
   hop_fb<1, PH, LV, HB>(g, u, p, ph, idx, aux);
@@ -110,6 +115,9 @@ k_mx_deo_dot(Geom g, LV u, const void* __restrict__ ph, const float2* __restrict
              float2* __restrict__ s, MixScal* sc, ReduceWs ws) {
   if (halted(sc)) return;
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx < g.sizeh) prefetch_links<0>(g, u, idx);   // as in k_mx_doe
+  pdl_wait();               // t from k_mx_doe
+  pdl_trigger();
   float v[1] = {0.0f};
   if (idx < g.sizeh) {
     const float m2 = float(sc->m2);
@@ -135,13 +143,23 @@ k_mx_deo_dot(Geom g, LV u, const void* __restrict__ ph, const float2* __restrict
 // beta = lambda / delta, delta = lambda.
 __global__ void k_mx_update(float4* __restrict__ xf, float4* __restrict__ r, const float4* __restrict__ p,
                             const float4* __restrict__ s, long n4, MixScal* sc, ReduceWs ws) {
-  if (halted(sc)) return;
+  if (halted(sc)) return;   // set by this kernel, four launches back
+  const long stride = long(gridDim.x) * blockDim.x;
+  // launched early: p, x_f and r are not written by k_mx_deo_dot; one lane
+  // in eight prefetches the 128-byte lines of its neighbours' elements
+  if ((threadIdx.x & 7) == 0)
+    for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n4; i += stride) {
+      prefetch_l2(p + i);
+      prefetch_l2(xf + i);
+      prefetch_l2(r + i);
+    }
+  pdl_wait();               // s and alpha from k_mx_deo_dot
+  pdl_trigger();
   const double delta = sc->delta;
   const double lm = sc->last_max > delta ? sc->last_max : delta;
   const bool rel = sc->every > 0 ? ((sc->iter + 1) % sc->every == 0) : (delta < sc->frac * lm);
   const float a = float(sc->alpha);
   float v[1] = {0.0f};
-  const long stride = long(gridDim.x) * blockDim.x;
   // two elements per pass, all loads issued before use
   for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n4; i += 2 * stride) {
     const long j = i + stride;
@@ -184,9 +202,13 @@ __global__ void k_mx_update(float4* __restrict__ xf, float4* __restrict__ r, con
 // p = r + beta p
 __global__ void k_mx_pupdate(float4* __restrict__ p, const float4* __restrict__ r, long n4, const MixScal* sc,
                              int guarded) {
-  if (guarded && halted(sc)) return;
-  const float b = float(sc->beta);
   const long stride = long(gridDim.x) * blockDim.x;
+  if (guarded && (threadIdx.x & 7) == 0)   // launched early: p is not written by k_mx_update
+    for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n4; i += stride) prefetch_l2(p + i);
+  pdl_wait();               // r, beta and the flags from k_mx_update
+  if (guarded && halted(sc)) return;
+  pdl_trigger();
+  const float b = float(sc->beta);
   for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n4; i += 2 * stride) {
     const long j = i + stride;
     float4 pv = p[i], rv = r[i], pw, rw;
@@ -314,8 +336,9 @@ void launch_mx_doe_t(int threads, const MixedBuffers& B, const MixScal* sc, cuda
   const int nb = blocks_for(g.sizeh, threads);
   with_sloppy_links(B, [&](const auto& u) {
     typedef typename std::decay<decltype(u)>::type LV;
-    if (B.ph32_mode == PH_SIGN8) k_mx_doe<PH_SIGN8, LV, HB><<<nb, threads, 0, st>>>(g, u, B.ph32, B.p, B.t, sc);
-    else k_mx_doe<PH_ANGLE, LV, HB><<<nb, threads, 0, st>>>(g, u, B.ph32, B.p, B.t, sc);
+    if (B.ph32_mode == PH_SIGN8)
+      launch_pdl(k_mx_doe<PH_SIGN8, LV, HB>, nb, threads, st, g, u, B.ph32, B.p, B.t, sc);
+    else launch_pdl(k_mx_doe<PH_ANGLE, LV, HB>, nb, threads, st, g, u, B.ph32, B.p, B.t, sc);
   });
 }
 
@@ -332,8 +355,8 @@ void launch_mx_deo_dot_t(const MixedBuffers& B, MixScal* sc, ReduceWs ws, cudaSt
   with_sloppy_links(B, [&](const auto& u) {
     typedef typename std::decay<decltype(u)>::type LV;
     if (B.ph32_mode == PH_SIGN8)
-      k_mx_deo_dot<PH_SIGN8, LV, HB><<<nb, MX_THREADS, 0, st>>>(g, u, B.ph32, B.t, B.p, B.s, sc, ws);
-    else k_mx_deo_dot<PH_ANGLE, LV, HB><<<nb, MX_THREADS, 0, st>>>(g, u, B.ph32, B.t, B.p, B.s, sc, ws);
+      launch_pdl(k_mx_deo_dot<PH_SIGN8, LV, HB>, nb, MX_THREADS, st, g, u, B.ph32, B.t, B.p, B.s, sc, ws);
+    else launch_pdl(k_mx_deo_dot<PH_ANGLE, LV, HB>, nb, MX_THREADS, st, g, u, B.ph32, B.t, B.p, B.s, sc, ws);
   });
 }
 
@@ -391,11 +414,10 @@ void enqueue_iteration(const MixedBuffers& B, MixScal* sc, cudaStream_t st) {
   launch_mx_doe(mx_doe_shape(B), B, sc, st);
   launch_mx_deo_dot(mx_deo_shape(B), B, sc, wsd, st);
   g_kernel_launches += 2;
-  k_mx_update<<<gr, RED_THREADS, 0, st>>>(reinterpret_cast<float4*>(B.xf), reinterpret_cast<float4*>(B.r),
-                                          reinterpret_cast<const float4*>(B.p),
-                                          reinterpret_cast<const float4*>(B.s), n4, sc, wsd);
-  k_mx_pupdate<<<gr, RED_THREADS, 0, st>>>(reinterpret_cast<float4*>(B.p), reinterpret_cast<const float4*>(B.r),
-                                           n4, sc, 1);
+  launch_pdl(k_mx_update, gr, RED_THREADS, st, reinterpret_cast<float4*>(B.xf), reinterpret_cast<float4*>(B.r),
+             reinterpret_cast<const float4*>(B.p), reinterpret_cast<const float4*>(B.s), n4, sc, wsd);
+  launch_pdl(k_mx_pupdate, gr, RED_THREADS, st, reinterpret_cast<float4*>(B.p), reinterpret_cast<const float4*>(B.r),
+             n4, static_cast<const MixScal*>(sc), 1);
   g_kernel_launches += 2;
 }
 

@@ -9,6 +9,7 @@
 #include <map>
 #include <mutex>
 #include <string>
+#include <cstdlib>
 #include "runtime.cuh"
 #include "../../include/ostaple_gb300.h"
 
@@ -16,6 +17,15 @@ namespace ost {
 
 static Runtime g_rt;
 unsigned long long g_kernel_launches = 0;
+
+bool pdl_enabled() {
+  static int on = -1;
+  if (on < 0) {
+    const char* e = getenv("OSTAPLE_PDL");
+    on = (e && e[0] == '0' && e[1] == 0) ? 0 : 1;
+  }
+  return on == 1;
+}
 Runtime& rt() { return g_rt; }
 
 static int g_err = 0;

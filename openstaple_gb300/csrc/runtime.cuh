@@ -47,6 +47,32 @@ extern unsigned long long g_kernel_launches;
 
 bool require_init(const char* who);
 
+// Programmatic dependent launch.  A kernel launched by launch_pdl may start
+// while the kernel before it on the stream is still running (its blocks are
+// scheduled once every block of that kernel has started or passed
+// pdl_trigger).  Such a kernel calls pdl_wait() before it reads anything the
+// previous kernel writes; it may read earlier before the wait only what
+// kernels at least two launches back wrote, and it calls pdl_trigger() only
+// after its own pdl_wait(), so a kernel two launches on finds every earlier
+// kernel complete.  Both are no-ops for a kernel launched without the
+// attribute.  OSTAPLE_PDL=0 in the environment launches without it.
+bool pdl_enabled();
+
+template <typename... P, typename... A>
+void launch_pdl(void (*kernel)(P...), int grid, int block, cudaStream_t st, A&&... args) {
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3(unsigned(grid));
+  cfg.blockDim = dim3(unsigned(block));
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = pdl_enabled() ? 1 : 0;
+  OST_CUDA(cudaLaunchKernelEx(&cfg, kernel, static_cast<P>(args)...));
+}
+
 // Host pointer -> device mirror (the OpenACC `present` table).  A pointer that
 // is not registered but already addresses device memory is used as is.
 // Returns nullptr (and records an error) if the pointer is neither.
