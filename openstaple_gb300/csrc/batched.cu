@@ -143,7 +143,9 @@ __global__ void __launch_bounds__(BT)
 k_b_doe(Geom g, LV u, const void* __restrict__ ph, const float2* __restrict__ p, float2* __restrict__ t, long vs,
         const BatchScal* sc) {
   typedef HopLayout<NS, SPL_> H;
-  if (!active_mask(sc)) return;
+  if (!active_mask(sc)) return;   // flags of k_b_update, two launches back
+  pdl_wait();                     // p from k_b_pupdate
+  pdl_trigger();
   int idx, sys[H::SPL];
   bool valid[H::SPL];
   const bool live = hop_thread<NS, SPL_>(g.sizeh, idx, sys, valid);
@@ -198,6 +200,8 @@ k_b_deo_dot(Geom g, LV u, const void* __restrict__ ph, const float2* __restrict_
             float2* __restrict__ s, long vs, BatchScal* sc, ReduceWs ws) {
   typedef HopLayout<NS> H;
   if (!active_mask(sc)) return;
+  pdl_wait();                     // t from k_b_doe
+  pdl_trigger();
   int idx, sys[H::SPL];
   bool valid[H::SPL];
   const bool live = hop_thread<NS>(g.sizeh, idx, sys, valid);
@@ -238,6 +242,8 @@ inline int seg_blocks(long n4, int nsys) {
 template <int NS>
 __global__ void k_b_update(float4* __restrict__ xf, float4* __restrict__ r, const float4* __restrict__ p,
                            const float4* __restrict__ s, long n4, long vs4, int bps, BatchScal* sc, ReduceWs ws) {
+  pdl_wait();                     // s and alpha from k_b_deo_dot
+  pdl_trigger();
   const int k = blockIdx.x / bps;
   const bool act = k < NS && batch_active(sc, k);
   bool rel = false;
@@ -304,6 +310,8 @@ __global__ void k_b_update(float4* __restrict__ xf, float4* __restrict__ r, cons
 template <int NS>
 __global__ void k_b_pupdate(float4* __restrict__ p, const float4* __restrict__ r, long n4, long vs4, int bps,
                             const BatchScal* sc) {
+  pdl_wait();                     // r, beta and the flags from k_b_update
+  pdl_trigger();
   const int k = blockIdx.x / bps;
   if (k >= NS || !batch_active(sc, k)) return;
   const float b = float(sc->beta[k]);
@@ -402,8 +410,10 @@ void launch_b_doe_spl(const BatchBuffers& B, BatchScal* sc, cudaStream_t st) {
   const int nb = hop_blocks<NS, SPL_>(g.sizeh);
   with_batch_links(B, [&](const auto& u) {
     typedef typename std::decay<decltype(u)>::type LV;
-    if (B.ph32_mode == PH_SIGN8) k_b_doe<NS, SPL_, PH_SIGN8, LV><<<nb, BT, 0, st>>>(g, u, B.ph32, B.p, B.t, n, sc);
-    else k_b_doe<NS, SPL_, PH_ANGLE, LV><<<nb, BT, 0, st>>>(g, u, B.ph32, B.p, B.t, n, sc);
+    if (B.ph32_mode == PH_SIGN8)
+      launch_pdl(k_b_doe<NS, SPL_, PH_SIGN8, LV>, nb, BT, st, g, u, B.ph32, B.p, B.t, n, static_cast<const BatchScal*>(sc));
+    else launch_pdl(k_b_doe<NS, SPL_, PH_ANGLE, LV>, nb, BT, st, g, u, B.ph32, B.p, B.t, n,
+                    static_cast<const BatchScal*>(sc));
   });
   OST_LAUNCH_CHECK();
 }
@@ -460,14 +470,14 @@ void enqueue_batch_iteration(const BatchBuffers& B, BatchScal* sc, cudaStream_t 
   with_batch_links(B, [&](const auto& u) {
     typedef typename std::decay<decltype(u)>::type LV;
     if (B.ph32_mode == PH_SIGN8)
-      k_b_deo_dot<NS, PH_SIGN8, LV><<<nb, BT, 0, st>>>(g, u, B.ph32, B.t, B.p, B.s, n, sc, wh);
-    else k_b_deo_dot<NS, PH_ANGLE, LV><<<nb, BT, 0, st>>>(g, u, B.ph32, B.t, B.p, B.s, n, sc, wh);
+      launch_pdl(k_b_deo_dot<NS, PH_SIGN8, LV>, nb, BT, st, g, u, B.ph32, B.t, B.p, B.s, n, sc, wh);
+    else launch_pdl(k_b_deo_dot<NS, PH_ANGLE, LV>, nb, BT, st, g, u, B.ph32, B.t, B.p, B.s, n, sc, wh);
   });
-  k_b_update<NS><<<NS * bps, RED_THREADS, 0, st>>>(reinterpret_cast<float4*>(B.xf), reinterpret_cast<float4*>(B.r),
-                                                    reinterpret_cast<const float4*>(B.p),
-                                                    reinterpret_cast<const float4*>(B.s), n4, n4, bps, sc, wh);
-  k_b_pupdate<NS><<<NS * bps, RED_THREADS, 0, st>>>(reinterpret_cast<float4*>(B.p),
-                                                     reinterpret_cast<const float4*>(B.r), n4, n4, bps, sc);
+  launch_pdl(k_b_update<NS>, NS * bps, RED_THREADS, st, reinterpret_cast<float4*>(B.xf),
+             reinterpret_cast<float4*>(B.r), reinterpret_cast<const float4*>(B.p),
+             reinterpret_cast<const float4*>(B.s), n4, n4, bps, sc, wh);
+  launch_pdl(k_b_pupdate<NS>, NS * bps, RED_THREADS, st, reinterpret_cast<float4*>(B.p),
+             reinterpret_cast<const float4*>(B.r), n4, n4, bps, static_cast<const BatchScal*>(sc));
 }
 
 // partial sums that the batched reductions need at most, for pre-sizing the
