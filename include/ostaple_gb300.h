@@ -315,6 +315,12 @@ int ostaple_mdagm_df(const su3_soa *u, const double_soa *phases, double mass, do
  * (inverter_package.u_f) are always used as given.  No reference
  * counterpart (the reference's sloppy links are FP32). */
 int ostaple_set_sloppy_links(int fmt);
+/* Host runs of the device-side link encoders, for tests without a GPU:
+ * q[i] = the biased 16-bit word of h[i] (rint(32768 h) clamped to +-32767,
+ * plus 32768); hi[i] = (float)x[i] and lo[i] = (float)(x[i] - (double)hi[i])
+ * as the double-float links compute them.  No reference counterpart. */
+int ostaple_q16_encode_host(const float *h, long n, unsigned *q);
+int ostaple_df_split_host(const double *x, long n, float *hi, float *lo);
 /* out = (m^2 + shift) in - D_eo D_oe in through the FP32 iteration kernels
  * with the current sloppy link format (FP32 in and out of the kernels, FP64
  * fields here): the operator of the FP32 iteration, exposed for testing.

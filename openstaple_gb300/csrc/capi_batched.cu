@@ -37,7 +37,7 @@ bool prepare(const Z* u64, const double* ph64, Prepared* out, cudaStream_t st) {
     if (!q) return false;
     uint4* a = reinterpret_cast<uint4*>(q);
     uint2* b = reinterpret_cast<uint2*>(q + 8 * 16 * size_t(sh));
-    links_to_q16(u64, a, b, sh, st);
+    links_to_q16(u32, a, b, sh, st);
     out->q16 = 1;
     out->uq = LinkQ16{a, b, sh};
   }

@@ -5,6 +5,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include "dslash.cuh"
+#include "dslash_df.cuh"
 #include "kernels.cuh"
 #include "mixed.cuh"
 #include "runtime.cuh"
@@ -52,7 +53,7 @@ bool prepare_f32(const Z* u64, const void* u_f, const double* ph64, PreparedF32*
       if (!q) return false;
       uint4* a = reinterpret_cast<uint4*>(q);
       uint2* b = reinterpret_cast<uint2*>(q + 8 * 16 * size_t(sh));
-      links_to_q16(u64, a, b, sh, st);
+      links_to_q16(u32, a, b, sh, st);
       out->q16 = 1;
       out->uq = LinkQ16{a, b, sh};
     }
@@ -104,6 +105,20 @@ int sloppy_links_q16() { return g_sloppy_q16; }
 }  // namespace ost
 
 extern "C" {
+
+// Host runs of the device encoders (same source), for tests without a GPU.
+int ostaple_q16_encode_host(const float* h, long n, unsigned* q) {
+  for (long i = 0; i < n; ++i) q[i] = q16_encode_f32(h[i]);
+  return 0;
+}
+
+int ostaple_df_split_host(const double* x, long n, float* hi, float* lo) {
+  for (long i = 0; i < n; ++i) {
+    hi[i] = float(x[i]);
+    lo[i] = df_lo_part(x[i], hi[i]);
+  }
+  return 0;
+}
 
 int ostaple_set_sloppy_links(int fmt) {
   const int prev = g_sloppy_q16;

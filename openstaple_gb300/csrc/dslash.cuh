@@ -10,6 +10,7 @@
 // The reference subtracts the four backward terms first, then adds the four
 // forward terms; the same order is kept here.
 #pragma once
+#include <cmath>
 #include <type_traits>
 #include "common.cuh"
 
@@ -91,8 +92,8 @@ OST_D void load_two_rows(const LinkView<C>& u, int dir, int idx, C m[6]) {
 }
 
 // Sloppy links in 16-bit fixed point: the first two rows of each link,
-// every real and imaginary part q = rint(32768 x) clamped to +-32767 and
-// stored biased as q + 32768 in 16 bits (real part in the low half of a
+// every real and imaginary part q = rint(32768 x) (x rounded to FP32 first)
+// clamped to +-32767 and stored biased as q + 32768 in 16 bits (real part in the low half of a
 // 32-bit word, imaginary part in the high half).  SU(3) entries lie in
 // [-1, 1], so the absolute error is at most 2^-16.  Per direction two
 // planes over the half lattice: `a` holds elements 0-3 of rows 0-1
@@ -112,10 +113,18 @@ OST_D float2 q16_decode(unsigned w) {
   return make_float2(fmaf(lo, 3.0517578125e-05f, -257.0f), fmaf(hi, 3.0517578125e-05f, -257.0f));
 }
 
-OST_HD unsigned q16_encode_part(double x) {
-  double q = rint(x * 32768.0);
-  q = q > 32767.0 ? 32767.0 : (q < -32767.0 ? -32767.0 : q);
-  return unsigned(int(q) + 32768);
+// q = rint(32768 h) of the FP32 rounding h of a link entry, clamped to
+// +-32767, biased by 32768 (the scaling is exact; the conversion rounds to
+// nearest even).  No FP64 arithmetic: on this part it runs at 1/64 of FP32.
+OST_HD unsigned q16_encode_f32(float h) {
+  const float y = h * 32768.0f;
+#ifdef __CUDA_ARCH__
+  int q = __float2int_rn(y);
+#else
+  int q = int(nearbyintf(y));
+#endif
+  q = q > 32767 ? 32767 : (q < -32767 ? -32767 : q);
+  return unsigned(q + 32768);
 }
 
 OST_D void load_two_rows(const LinkQ16& u, int dir, int idx, float2 m[6]) {

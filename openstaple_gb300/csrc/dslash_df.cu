@@ -201,7 +201,7 @@ __global__ void k_links_lo(const double2* __restrict__ u64, float2* __restrict__
     const long dir = i / (6 * sh), rem = i - dir * 6 * sh;
     const double2 v = __ldcs(u64 + dir * 9 * sh + rem);
     const float hx = float(v.x), hy = float(v.y);
-    u_lo[i] = make_float2(float(v.x - double(hx)), float(v.y - double(hy)));
+    u_lo[i] = make_float2(df_lo_part(v.x, hx), df_lo_part(v.y, hy));
   }
 }
 

@@ -10,6 +10,7 @@
 // is still computed in native FP64.
 #pragma once
 #include <cuda_runtime.h>
+#include <cstring>
 #include "common.cuh"
 
 namespace ost {
@@ -34,6 +35,40 @@ struct DfWork {
 // lo parts of the compact links: lo = (float)(u - (double)(float)u), the hi
 // parts being the existing compact FP32 copy.
 void links_to_lo_compact(const double2* u64, float2* u_lo, long sizeh, cudaStream_t st);
+
+// lo = (float)(x - (double)hi) for hi = (float)x, without FP64 arithmetic
+// (1/64 of the FP32 rate on this part): with x = m 2^(e-1075) (m the 53-bit
+// mantissa) and hi = mh 2^(eh-150), the difference d = m - mh 2^(eh-e+925)
+// is an exact integer of at most 30 bits; lo = (float)d 2^(e-1075) rounds
+// once, like the FP64 expression, and the power of two is exact while
+// 2^(e-1075) is a normal float.  Zero, tiny and huge x take the FP64 route.
+OST_HD float df_lo_part(double x, float hi) {
+  unsigned long long b;
+  unsigned hb;
+#ifdef __CUDA_ARCH__
+  b = (unsigned long long)__double_as_longlong(x);
+  hb = __float_as_uint(hi);
+#else
+  memcpy(&b, &x, sizeof(b));
+  memcpy(&hb, &hi, sizeof(hb));
+#endif
+  const int e = int((b >> 52) & 0x7FF);
+  if (e < 1075 - 126 + 30 || e > 1023 + 100) return float(x - double(hi));
+  const long long m = (long long)((b & 0xFFFFFFFFFFFFFull) | (1ull << 52));
+  const int eh = int((hb >> 23) & 0xFF);
+  const long long mh = (long long)((hb & 0x7FFFFFu) | 0x800000u);
+  const long long d = m - (mh << (eh - e + 925));
+  if (d == 0) return 0.0f;   // x - hi = +0 in FP64, whatever the sign of x
+  const unsigned pb = unsigned(e - 1075 + 127) << 23;   // 2^(e-1075) as a float
+  float p2;
+#ifdef __CUDA_ARCH__
+  p2 = __uint_as_float(pb);
+#else
+  memcpy(&p2, &pb, sizeof(p2));
+#endif
+  const float lo = float(int(d)) * p2;
+  return (b >> 63) ? -lo : lo;
+}
 
 // Operator and work fields for a solve on the current lattice: computes the
 // lo link parts from the FP64 links (workspace slots WS_LINKS_LO and WS_DF).

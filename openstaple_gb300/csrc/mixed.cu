@@ -40,23 +40,26 @@ void links_to_f32_compact(const double2* u64, float2* u32, long sh, cudaStream_t
   OST_LAUNCH_CHECK();
 }
 
-__global__ void k_links_q16(const double2* __restrict__ u64, uint4* __restrict__ a, uint2* __restrict__ b, long sh) {
+// one thread per (direction, site): the six FP32 entries of the two rows
+// (compact layout [dir][6][sizeh]) -> the link's 16- and 8-byte words
+__global__ void k_links_q16(const float2* __restrict__ u32, uint4* __restrict__ a, uint2* __restrict__ b, long sh) {
   const long n = 8L * sh;
   for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n; i += long(gridDim.x) * blockDim.x) {
-    const long dir = i / sh, idx = i - dir * sh;
+    const int dir = int(i / sh);
+    const long idx = i - long(dir) * sh;
     unsigned w[6];
 #pragma unroll
     for (int k = 0; k < 6; ++k) {
-      const double2 v = __ldcs(u64 + (dir * 9 + k) * sh + idx);
-      w[k] = q16_encode_part(v.x) | (q16_encode_part(v.y) << 16);
+      const float2 v = __ldcs(u32 + (long(dir) * 6 + k) * sh + idx);
+      w[k] = q16_encode_f32(v.x) | (q16_encode_f32(v.y) << 16);
     }
     a[i] = make_uint4(w[0], w[1], w[2], w[3]);
     b[i] = make_uint2(w[4], w[5]);
   }
 }
 
-void links_to_q16(const double2* u64, uint4* a, uint2* b, long sh, cudaStream_t st) {
-  k_links_q16<<<8 * rt().num_sms, 256, 0, st>>>(u64, a, b, sh);
+void links_to_q16(const float2* u32, uint4* a, uint2* b, long sh, cudaStream_t st) {
+  k_links_q16<<<8 * rt().num_sms, 256, 0, st>>>(u32, a, b, sh);
   OST_LAUNCH_CHECK();
 }
 

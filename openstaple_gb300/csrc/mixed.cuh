@@ -74,9 +74,9 @@ struct MixedBuffers {
 
 // Converts the first two rows of FP64 su3_soa[8] links to a compact FP32 copy.
 void links_to_f32_compact(const double2* u64, float2* u32, long sizeh, cudaStream_t st);
-// Converts the first two rows of FP64 su3_soa[8] links to the 16-bit
+// Converts the compact FP32 links (links_to_f32_compact) to the 16-bit
 // fixed-point planes of LinkQ16 (a: 8 x sizeh uint4, b: 8 x sizeh uint2).
-void links_to_q16(const double2* u64, uint4* a, uint2* b, long sizeh, cudaStream_t st);
+void links_to_q16(const float2* u32, uint4* a, uint2* b, long sizeh, cudaStream_t st);
 // Sign bytes from FP64 phase angles; *all_exact (device int) is cleared when
 // some angle is neither 0 nor pi.
 void phases_to_signs(const double* ph64, unsigned char* sg, int* all_exact, long sizeh, cudaStream_t st);

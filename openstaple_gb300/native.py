@@ -115,6 +115,8 @@ SIGNATURES = {
     "l2norm2_global": (_D, [_P]),
     "ostaple_mdagm_df": (_I, [_P, _P, _D, _D, _P, _P]),
     "ostaple_set_sloppy_links": (_I, [_I]),
+    "ostaple_q16_encode_host": (_I, [_P, C.c_long, _P]),
+    "ostaple_df_split_host": (_I, [_P, C.c_long, _P, _P]),
     "ostaple_mdagm_sloppy": (_I, [_P, _P, _D, _D, _P, _P]),
     "ostaple_net_weights_save": (_I, [C.c_char_p, _P]),
     "ostaple_net_weights_load": (_I, [C.c_char_p, _P]),

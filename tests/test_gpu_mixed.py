@@ -109,9 +109,11 @@ def test_mixed_with_generic_phases(lat_factory):
 
 def quantize_links_q16(u):
     """The 16-bit fixed-point sloppy links as the FP32 kernels see them: the
-    first two rows rounded to multiples of 2^-15 (half to even, clamped to
-    +-32767/32768), the third row rebuilt as conj(row0 x row1)."""
-    q = np.clip(np.rint(u.real * 32768.0), -32767, 32767) + 1j * np.clip(np.rint(u.imag * 32768.0), -32767, 32767)
+    first two rows rounded to FP32, then to multiples of 2^-15 (half to even,
+    clamped to +-32767/32768), the third row rebuilt as conj(row0 x row1)."""
+    re = u.real.astype(np.float32).astype(np.float64)
+    im = u.imag.astype(np.float32).astype(np.float64)
+    q = np.clip(np.rint(re * 32768.0), -32767, 32767) + 1j * np.clip(np.rint(im * 32768.0), -32767, 32767)
     q = q / 32768.0
     a, c = q[:, 0], q[:, 1]
     q[:, 2] = np.conj(np.stack([a[:, 1] * c[:, 2] - a[:, 2] * c[:, 1],
