@@ -22,14 +22,17 @@ struct Prepared {
   int mode;
   int q16;        // 16-bit links for the batched FP32 iteration (the CG-M phase keeps u32)
   LinkQ16 uq;
+  const float2* lo;   // lo parts of the double-float links
 };
 
 bool prepare(const Z* u64, const double* ph64, Prepared* out, cudaStream_t st) {
   const long sh = rt().g.sizeh;
   float2* u32 = static_cast<float2*>(workspace(WS_LINKS_F32, sizeof(float2) * 48 * size_t(sh)));
+  float2* lo = static_cast<float2*>(workspace(WS_LINKS_LO, sizeof(float2) * 48 * size_t(sh)));
   char* sg = static_cast<char*>(workspace(WS_SIGNS, 256 + 8 * size_t(sh) * sizeof(float)));
-  if (!u32 || !sg) return false;
-  links_to_f32_compact(u64, u32, sh, st);
+  if (!u32 || !lo || !sg) return false;
+  links_to_f32_compact(u64, u32, sh, st, lo);
+  out->lo = lo;
   out->q16 = 0;
   out->uq = LinkQ16{nullptr, nullptr, sh};
   if (sloppy_links_q16()) {
@@ -111,7 +114,7 @@ int ostaple_invert_mixed_batch(const su3_soa* u, const double_soa* phases, doubl
   DfOperator dop{};
   DfWork dwk{};
   const int use_df = pr.mode == PH_SIGN8 &&
-                     df_prepare(u64, pr.u32, static_cast<const unsigned char*>(pr.ph), &dop, &dwk, st);
+                     df_prepare(pr.u32, pr.lo, static_cast<const unsigned char*>(pr.ph), &dop, &dwk);
   int ok = 1;
   for (int s0 = 0; s0 < nsys; s0 += BATCH_MAX) {
     const int m = std::min(BATCH_MAX, nsys - s0);
@@ -190,7 +193,7 @@ int ostaple_multishift_batch(const su3_soa* u, const double_soa* phases, double 
   DfOperator dop{};
   DfWork dwk{};
   const int use_df = pr.mode == PH_SIGN8 &&
-                     df_prepare(u64, pr.u32, static_cast<const unsigned char*>(pr.ph), &dop, &dwk, st);
+                     df_prepare(pr.u32, pr.lo, static_cast<const unsigned char*>(pr.ph), &dop, &dwk);
   int ok = 1;
   std::vector<int> sys_rhs, sys_shift;
   for (int k = 0; k < order; ++k)

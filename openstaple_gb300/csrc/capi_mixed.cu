@@ -25,6 +25,7 @@ struct PreparedF32 {
   int mode;
   int q16;
   LinkQ16 uq;
+  const float2* lo;   // lo parts of the double-float links (library-converted links only)
 };
 
 int g_sloppy_q16 = 1;
@@ -37,15 +38,18 @@ bool prepare_f32(const Z* u64, const void* u_f, const double* ph64, PreparedF32*
   const long sh = rt().g.sizeh;
   out->q16 = 0;
   out->uq = LinkQ16{nullptr, nullptr, sh};
+  out->lo = nullptr;
   if (u_f) {
     out->u32 = static_cast<const float2*>(resolve(u_f, "u_f"));
     if (!out->u32) return false;
     out->compact = 0;
   } else {
     float2* u32 = static_cast<float2*>(workspace(WS_LINKS_F32, sizeof(float2) * 48 * size_t(sh)));
-    if (!u32) return false;
-    links_to_f32_compact(u64, u32, sh, st);
+    float2* lo = static_cast<float2*>(workspace(WS_LINKS_LO, sizeof(float2) * 48 * size_t(sh)));
+    if (!u32 || !lo) return false;
+    links_to_f32_compact(u64, u32, sh, st, lo);
     out->u32 = u32;
+    out->lo = lo;
     out->compact = 1;
     if (g_sloppy_q16) {
       // 8 directions x (16 + 8) bytes per half-lattice site
@@ -83,7 +87,7 @@ bool prepare_f32(const Z* u64, const void* u_f, const double* ph64, PreparedF32*
 // and the library's own compact FP32 links.
 bool prepare_df(const Z* u64, const PreparedF32& pf, DfOperator* op, DfWork* w, cudaStream_t st) {
   if (pf.mode != PH_SIGN8 || !pf.compact) return false;
-  return df_prepare(u64, pf.u32, static_cast<const unsigned char*>(pf.ph), op, w, st);
+  return df_prepare(pf.u32, pf.lo, static_cast<const unsigned char*>(pf.ph), op, w);
 }
 
 template <typename T>

@@ -191,37 +191,19 @@ __global__ void k_df_split(const double2* __restrict__ x, float2* __restrict__ h
     const double2 v = x[i];
     const float hx = float(v.x), hy = float(v.y);
     hi[i] = make_float2(hx, hy);
-    lo[i] = make_float2(float(v.x - double(hx)), float(v.y - double(hy)));
-  }
-}
-
-__global__ void k_links_lo(const double2* __restrict__ u64, float2* __restrict__ u_lo, long sh) {
-  const long n = 8L * 6 * sh;
-  for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n; i += long(gridDim.x) * blockDim.x) {
-    const long dir = i / (6 * sh), rem = i - dir * 6 * sh;
-    const double2 v = __ldcs(u64 + dir * 9 * sh + rem);
-    const float hx = float(v.x), hy = float(v.y);
-    u_lo[i] = make_float2(df_lo_part(v.x, hx), df_lo_part(v.y, hy));
+    lo[i] = make_float2(df_lo_part(v.x, hx), df_lo_part(v.y, hy));
   }
 }
 
 }  // namespace
 
-void links_to_lo_compact(const double2* u64, float2* u_lo, long sh, cudaStream_t st) {
-  k_links_lo<<<8 * rt().num_sms, 256, 0, st>>>(u64, u_lo, sh);
-  OST_LAUNCH_CHECK();
-}
-
-bool df_prepare(const double2* u64, const float2* u_hi, const unsigned char* signs, DfOperator* op, DfWork* w,
-                cudaStream_t st) {
+bool df_prepare(const float2* u_hi, const float2* u_lo, const unsigned char* signs, DfOperator* op, DfWork* w) {
   const long sh = rt().g.sizeh;
   const size_t n = 3 * size_t(sh);
-  float2* lo = static_cast<float2*>(workspace(WS_LINKS_LO, sizeof(float2) * 48 * size_t(sh)));
   float2* wk = static_cast<float2*>(workspace(WS_DF, sizeof(float2) * 4 * n));
-  if (!lo || !wk) return false;
-  links_to_lo_compact(u64, lo, sh, st);
+  if (!wk || !u_hi || !u_lo) return false;
   op->u_hi = u_hi;
-  op->u_lo = lo;
+  op->u_lo = u_lo;
   op->signs = signs;
   w->x_hi = wk;
   w->x_lo = wk + n;

@@ -32,10 +32,6 @@ struct DfWork {
   float2* t_lo;
 };
 
-// lo parts of the compact links: lo = (float)(u - (double)(float)u), the hi
-// parts being the existing compact FP32 copy.
-void links_to_lo_compact(const double2* u64, float2* u_lo, long sizeh, cudaStream_t st);
-
 // lo = (float)(x - (double)hi) for hi = (float)x, without FP64 arithmetic
 // (1/64 of the FP32 rate on this part): with x = m 2^(e-1075) (m the 53-bit
 // mantissa) and hi = mh 2^(eh-150), the difference d = m - mh 2^(eh-e+925)
@@ -70,11 +66,10 @@ OST_HD float df_lo_part(double x, float hi) {
   return (b >> 63) ? -lo : lo;
 }
 
-// Operator and work fields for a solve on the current lattice: computes the
-// lo link parts from the FP64 links (workspace slots WS_LINKS_LO and WS_DF).
-// u_hi: the compact FP32 links (hi parts), signs: one sign byte per link.
-bool df_prepare(const double2* u64, const float2* u_hi, const unsigned char* signs, DfOperator* op, DfWork* w,
-                cudaStream_t st);
+// Operator and work fields (workspace slot WS_DF) for a solve on the current
+// lattice.  u_hi / u_lo: the compact FP32 links and their lo parts, both
+// written by links_to_f32_compact; signs: one sign byte per link.
+bool df_prepare(const float2* u_hi, const float2* u_lo, const unsigned char* signs, DfOperator* op, DfWork* w);
 
 // out = (m2 + shift) in - D_eo D_oe in, in double-float arithmetic; in and
 // out are FP64 vec3 fields on the even sites.  Needs exact phases (signs).

@@ -26,17 +26,27 @@ static constexpr int MX_THREADS = 128;
 OST_D bool halted(const MixScal* s) { return (*(volatile const int*)&s->done) | (*(volatile const int*)&s->need_rel); }
 
 // ---- preparation kernels ----
-__global__ void k_links_f32(const double2* __restrict__ u64, float2* __restrict__ u32, long sh) {
-  const long n = 8L * 6 * sh;
-  for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n; i += long(gridDim.x) * blockDim.x) {
-    long dir = i / (6 * sh), rem = i - dir * 6 * sh;   // rem indexes rows 0..1 (6 arrays)
-    double2 v = __ldcs(u64 + dir * 9 * sh + rem);
-    u32[i] = make_float2(float(v.x), float(v.y));
+// blockIdx.y = link plane (direction x 6 entries of rows 0-1); x runs over
+// the half lattice.  With u_lo, also the lo parts of the double-float links
+// from the same FP64 loads.
+__global__ void k_links_f32(const double2* __restrict__ u64, float2* __restrict__ u32, float2* __restrict__ u_lo,
+                            long sh) {
+  const int plane = blockIdx.y;
+  const int dir = plane / 6, k = plane - 6 * (plane / 6);
+  const double2* src = u64 + (long(dir) * 9 + k) * sh;
+  float2* hi = u32 + long(plane) * sh;
+  float2* lo = u_lo ? u_lo + long(plane) * sh : nullptr;
+  for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < sh; i += long(gridDim.x) * blockDim.x) {
+    const double2 v = __ldcs(src + i);
+    const float hx = float(v.x), hy = float(v.y);
+    hi[i] = make_float2(hx, hy);
+    if (lo) lo[i] = make_float2(df_lo_part(v.x, hx), df_lo_part(v.y, hy));
   }
 }
 
-void links_to_f32_compact(const double2* u64, float2* u32, long sh, cudaStream_t st) {
-  k_links_f32<<<8 * rt().num_sms, 256, 0, st>>>(u64, u32, sh);
+void links_to_f32_compact(const double2* u64, float2* u32, long sh, cudaStream_t st, float2* u_lo) {
+  const long bx = (sh + 255) / 256;
+  k_links_f32<<<dim3(unsigned(bx < 128 ? bx : 128), 48), 256, 0, st>>>(u64, u32, u_lo, sh);
   OST_LAUNCH_CHECK();
 }
 

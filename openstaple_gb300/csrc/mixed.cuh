@@ -72,8 +72,10 @@ struct MixedBuffers {
   DfWork dfw;
 };
 
-// Converts the first two rows of FP64 su3_soa[8] links to a compact FP32 copy.
-void links_to_f32_compact(const double2* u64, float2* u32, long sizeh, cudaStream_t st);
+// Converts the first two rows of FP64 su3_soa[8] links to a compact FP32 copy
+// ([dir][6][sizeh]); with u_lo (same layout) also the lo parts
+// (float)(u - (double)(float)u) of the double-float links.
+void links_to_f32_compact(const double2* u64, float2* u32, long sizeh, cudaStream_t st, float2* u_lo = nullptr);
 // Converts the compact FP32 links (links_to_f32_compact) to the 16-bit
 // fixed-point planes of LinkQ16 (a: 8 x sizeh uint4, b: 8 x sizeh uint2).
 void links_to_q16(const float2* u32, uint4* a, uint2* b, long sizeh, cudaStream_t st);
