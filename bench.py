@@ -380,7 +380,8 @@ def main():
         h2d = ue.nbytes + phe.nbytes + be.nbytes + xe.nbytes
         d2h = xe.nbytes
         times = []
-        for k in range(args.warmup + args.steps):
+        e2e_steps = max(args.steps, 9)   # enough steps for a median that host stalls do not move
+        for k in range(args.warmup + e2e_steps):
             xe[...] = 0
             barrier()
             t0 = time.perf_counter()
@@ -398,9 +399,10 @@ def main():
                 times.append(dt)
         for a in (ue, phe, be, xe):
             lat.release(a)
-        # the median of the timed steps: a single host-side stall of a step
-        # (seen as one 60-70 ms step among 28 ms ones on some boxes) would
-        # otherwise dominate a mean of a few steps; every step is listed
+        # the median of the timed steps: host-side stalls of single steps
+        # (seen as 40-70 ms steps among 28 ms ones on some boxes, where the
+        # host memory is shared with other jobs) would otherwise dominate a
+        # mean of a few steps; every step is listed
         e2e_ms = max_over_ranks(1e3 * float(np.median(times)), world)
         e2e = {"value": world * nrhs * 1e3 / e2e_ms, "unit": "solves/s", "ms_per_step": e2e_ms,
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
