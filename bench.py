@@ -50,6 +50,53 @@ BYTES_Q16_DEO = 8 * 12 * 2 + 8 * 1 + 2 * 3 * 8 + 3 * 8        # = 272
 BYTES_F64_ANGLE = 8 * 12 * 8 + 8 * 8 + 3 * 16 + 3 * 16   # links(2 rows) + angles + in + out = 928
 
 
+def run_multishift(api, L, lat, u, ph, b, dims, rank, stream, args):
+    import torch
+    from openstaple_gb300 import fields as F
+    apx = json.loads((ROOT / "tests" / "golden" / "ratapprox.json").read_text())["order19"]
+    mx = 64.0 * 1.05
+    eps = mx ** (apx["exponent_num"] / apx["exponent_den"])
+    ra = api.make_approx(apx["a0"] * eps, np.array(apx["a"]) * mx * eps, np.array(apx["b"]) * mx)
+    order = ra.approx_order
+    bm = np.stack([b] + [F.gaussian_vec3(dims, args.seed + 17 * rank + 200 + k) for k in range(3)])
+    xm = lat.vec3(4 * order)
+    lat.present(bm)
+    lat.present(xm)
+
+    def timed(f):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        r = f()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1), r
+
+    runs = [timed(lambda: api.multishift_batch(u, ph, args.mass, ra, bm, xm, args.res, 100000, args.delta))
+            for _ in range(2)]
+    ms, info = min(runs, key=lambda t: t[0])
+    # the reference algorithm in FP64 on the GPU, one source after the other
+    work = [lat.vec3() for _ in range(4)]
+    sf, xo = lat.vec3(order), lat.vec3(order)
+    for a in work + [sf, xo]:
+        lat.present(a, copy=False)
+    fp = api.make_ferm_param(args.mass, ph)
+    fp64_ms, fp64_iters = 0.0, []
+    for k in range(4):
+        bk = np.ascontiguousarray(bm[k])
+        lat.present(bk)
+        t, (st, n) = timed(lambda: api.multishift_invert(u, fp, ra, xo, bk, args.res, *work, sf, 100000))
+        fp64_ms += t
+        fp64_iters.append(int(n))
+        lat.release(bk)
+    for a in work + [sf, xo, bm, xm]:
+        lat.release(a)
+    return {"sources": 4, "shifts": int(order), "ms": ms, "status": int(info["status"]),
+            "true_residual_max": float(info["true_res"].max()), "cgm_iterations": [int(i) for i in info["iters_cgm"]],
+            "fp64_multishift_invert_ms": fp64_ms, "fp64_iterations": fp64_iters,
+            "speedup_vs_fp64_multishift_invert": fp64_ms / ms if ms else None}
+
+
 def parse_args():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -72,6 +119,10 @@ def parse_args():
                     help="right-hand sides per step; >1 solves them together with the batched solver")
     ap.add_argument("--links", choices=("q16", "f32"), default="q16",
                     help="sloppy link format of the FP32 iteration (16-bit fixed point or FP32 rows)")
+    ap.add_argument("--every", type=int, default=0,
+                    help="reliable update every N iterations of the single-system solver (0: the delta criterion)")
+    ap.add_argument("--no-multishift", action="store_true",
+                    help="skip the 4-source x 19-shift multi-shift measurement reported beside the headline")
     ap.add_argument("--delta", type=float, default=1e-4,
                     help="reliable update when |r|^2 < delta * max|r|^2 since the last one")
     return ap.parse_args()
@@ -300,7 +351,7 @@ def main():
             return dict(status=r["status"], iters=int(r["iters"].max()), true_res=float(r["true_res"].max()),
                         n_reliable=int(r["n_reliable"].max()))
         L.set_vec3_soa_to_zero(x.ctypes.data)
-        return api.invert_mixed(u, ph, args.mass, 0.0, x, b, args.res, 100000, 0, args.delta)
+        return api.invert_mixed(u, ph, args.mass, 0.0, x, b, args.res, 100000, args.every, args.delta)
 
     # the same workload with 4 right-hand sides solved together (reported beside the headline)
     batched4 = None
@@ -325,6 +376,17 @@ def main():
                     "true_residual_max": float(r4["true_res"].max())}
         lat.release(b4)
         lat.release(x4)
+
+    # the batched multi-shift workload: 4 sources x the 19 shifts of the
+    # order-19 x^(-1/4) approximation (rescaled to [lambda_min, 64 * 1.05]),
+    # every system to an FP64 true residual of 1e-10, against the reference
+    # algorithm (multishift_invert, FP64) on the GPU, one source at a time
+    multishift = None
+    if nrhs == 1 and not args.skip_fp64 and args.solver == "mixed" and not args.no_multishift:
+        try:
+            multishift = run_multishift(api, L, lat, u, ph, b, dims, rank, stream, args)
+        except Exception as exc:   # reported, never fatal to the headline line
+            multishift = {"error": str(exc)[:200]}
 
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clk:
@@ -392,7 +454,7 @@ def main():
             elif nrhs > 1:
                 api.invert_mixed_batch(ue, phe, args.mass, xe, be, None, args.res, 100000, args.delta)
             else:
-                api.invert_mixed(ue, phe, args.mass, 0.0, xe, be, args.res, 100000, 0, args.delta)
+                api.invert_mixed(ue, phe, args.mass, 0.0, xe, be, args.res, 100000, args.every, args.delta)
             lat.update_host(xe)
             dt = time.perf_counter() - t0
             if k >= args.warmup:
@@ -430,6 +492,8 @@ def main():
                        "learned": learned,
                        "rhs_per_step": nrhs,
                        "batched_4rhs": batched4,
+                       "multishift_4x19": multishift,
+                       "reliable_every": args.every,
                        "iterations": infos[-1]["iters"], "reliable_updates": infos[-1]["n_reliable"],
                        "true_residual": infos[-1]["true_res"], "all_converged": ok,
                        "plain_fp64_cg": {"ms": fp64["ms"], "iterations": fp64["iters"], "status": fp64["status"]},
