@@ -58,3 +58,23 @@ def test_init_without_gpu_fails_cleanly(built):
     # odd extents are rejected before touching the device
     assert L.ostaple_init(5, 4, 4, 4) == -6
     L.ostaple_clear_error()
+
+
+def test_host_switches_without_a_gpu(built):
+    """The launch-shape autotuner and the sloppy-link format are host state:
+    they can be set and read back on a machine without a GPU."""
+    from openstaple_gb300 import api
+    from openstaple_gb300.native import lib
+    L = lib()
+    assert api.autotune_report() == ""          # nothing tuned in this process
+    api.autotune(False)
+    api.autotune(2 + 3)                          # forced candidate (tests)
+    api.autotune(True)
+    assert api.autotune_report() == ""
+    prev = api.set_sloppy_links("f32")
+    assert prev == "q16"                         # the default
+    assert api.set_sloppy_links("q16") == "f32"
+    assert L.ostaple_set_sloppy_links(1) == 1
+    import pytest
+    with pytest.raises(ValueError):
+        api.set_sloppy_links("fp16")
