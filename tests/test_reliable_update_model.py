@@ -28,11 +28,25 @@ def quantise_q16(u):
     return np.ascontiguousarray(q)
 
 
-def mixed_cg_model(o, u, ph, b, every, hestenes_stiefel, max_iter):
-    """FP32 CG on the sloppy operator with FP64 reliable updates every
-    `every` iterations; returns (iterations, FP64 true relative residual)."""
+def quantise(u, fmt):
+    if fmt == "q16":
+        return quantise_q16(u)
+    dt = {"f32": np.float32, "f16": np.float16}[fmt]
+    q = u.real.astype(dt).astype(np.float64) + 1j * u.imag.astype(dt).astype(np.float64)
+    a, c = q[:, 0], q[:, 1]
+    q[:, 2] = np.conj(np.stack([a[:, 1] * c[:, 2] - a[:, 2] * c[:, 1],
+                                a[:, 2] * c[:, 0] - a[:, 0] * c[:, 2],
+                                a[:, 0] * c[:, 1] - a[:, 1] * c[:, 0]], axis=1))
+    return np.ascontiguousarray(q)
+
+
+def mixed_cg_model(o, u, ph, b, every, hestenes_stiefel, max_iter, fmt="q16", delta_frac=None):
+    """FP32 CG on the sloppy operator (links in format fmt) with FP64
+    reliable updates every `every` iterations, or, with delta_frac, when
+    |r|^2 < delta_frac * max|r|^2 since the last one; returns (iterations,
+    FP64 true relative residual)."""
     m2 = MASS * MASS
-    uq = quantise_q16(u)
+    uq = quantise(u, fmt)
     a32 = lambda v: o.mdagm(uq, np.ascontiguousarray(v.astype(np.complex128)), ph, m2).astype(np.complex64)
     a64 = lambda v: o.mdagm(u, np.ascontiguousarray(v), ph, m2)
     dot = lambda x, y: float(np.sum(x.real.astype(np.float64) * y.real + x.imag.astype(np.float64) * y.imag))
@@ -42,6 +56,7 @@ def mixed_cg_model(o, u, ph, b, every, hestenes_stiefel, max_iter):
     p = r.copy()
     xf = np.zeros_like(r)
     delta = dot(r, r)
+    rmax = delta
     it = 0
     while it < max_iter:
         s = a32(p)
@@ -49,7 +64,9 @@ def mixed_cg_model(o, u, ph, b, every, hestenes_stiefel, max_iter):
         alpha = delta / pap
         it += 1
         xf = (xf + np.float32(alpha) * p).astype(np.complex64)
-        if it % every == 0:
+        rmax = max(rmax, delta)
+        due = (delta < delta_frac * rmax) if delta_frac else (it % every == 0)
+        if due or delta < (0.9e-10) ** 2 * bn:
             x = x + xf.astype(np.complex128)
             xf[:] = 0
             r64 = b - a64(x)
@@ -60,6 +77,7 @@ def mixed_cg_model(o, u, ph, b, every, hestenes_stiefel, max_iter):
             lam = dot(r64, r64)
             beta = -dot(r, s) / pap if hestenes_stiefel else lam / delta
             delta = lam
+            rmax = lam
             p = (r + np.float32(beta) * p).astype(np.complex64)
             continue
         r = (r - np.float32(alpha) * s).astype(np.complex64)
@@ -82,3 +100,25 @@ def test_hestenes_stiefel_beta_keeps_the_fixed_interval_solve_converging():
     assert res_hs < 1e-10 and it_hs <= 200, (it_hs, res_hs)
     it_ref, res_ref = mixed_cg_model(o, u, ph, b, 50, False, 400)
     assert res_ref > 1e-6, (it_ref, res_ref)   # stalls far above the target
+
+
+def test_sixteen_bit_fixed_point_links_converge_like_fp32():
+    """16-bit fixed-point links need about the FP32 links' iteration count at
+    the benchmark's reliable-update criterion (|r|^2 < 1e-4 max|r|^2) and at
+    a criterion 10^4 times tighter; FP16 links (the same 24 bytes per link)
+    need more at the tighter one, and with the reference's beta they do not
+    converge there at all."""
+    from oracle import Oracle
+    o = Oracle(DIMS)
+    u = F.random_su3_links(DIMS, 81)
+    ph = F.staggered_phases(DIMS)
+    b = F.gaussian_vec3(DIMS, 82)
+    it32, res32 = mixed_cg_model(o, u, ph, b, 0, True, 400, "f32", 1e-4)
+    assert res32 < 1e-10, (it32, res32)
+    for frac in (1e-4, 1e-8):
+        it16, res16 = mixed_cg_model(o, u, ph, b, 0, True, 400, "q16", frac)
+        assert res16 < 1e-10 and it16 <= 1.1 * it32 + 5, (frac, it16, it32)
+    it_h, res_h = mixed_cg_model(o, u, ph, b, 0, True, 400, "f16", 1e-8)
+    assert res_h < 1e-10 and it_h > it16, (it_h, it16)
+    it_r, res_r = mixed_cg_model(o, u, ph, b, 0, False, 4 * it32, "f16", 1e-8)
+    assert res_r > 1e-10, (it_r, res_r)
