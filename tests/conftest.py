@@ -43,5 +43,27 @@ def relerr(a, b) -> float:
     return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
 
 
+def rebuild_row2(q):
+    """Row 2 of su3_soa links as conj(row0 x row1), the kernels' rebuild."""
+    a, c = q[:, 0], q[:, 1]
+    q[:, 2] = np.conj(np.stack([a[:, 1] * c[:, 2] - a[:, 2] * c[:, 1],
+                                a[:, 2] * c[:, 0] - a[:, 0] * c[:, 2],
+                                a[:, 0] * c[:, 1] - a[:, 1] * c[:, 0]], axis=1))
+    return np.ascontiguousarray(q)
+
+
+def quantise_links(u, fmt):
+    """The sloppy links as the FP32 kernels see them.  "q16": rows 0-1
+    rounded to FP32, then to multiples of 2^-15 (half to even, clamped to
+    +-32767/32768); "f32" / "f16": rows 0-1 rounded to that type; row 2
+    rebuilt in every case."""
+    if fmt == "q16":
+        re = np.clip(np.rint(u.real.astype(np.float32).astype(np.float64) * 32768.0), -32767, 32767)
+        im = np.clip(np.rint(u.imag.astype(np.float32).astype(np.float64) * 32768.0), -32767, 32767)
+        return rebuild_row2((re + 1j * im) / 32768.0)
+    dt = {"f32": np.float32, "f16": np.float16}[fmt]
+    return rebuild_row2(u.real.astype(dt).astype(np.float64) + 1j * u.imag.astype(dt).astype(np.float64))
+
+
 def load_golden(tag: str):
     return dict(np.load(GOLDEN / f"dirac_{tag}.npz"))

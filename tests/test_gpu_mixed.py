@@ -5,7 +5,7 @@ implies (1e-8 relative here)."""
 import numpy as np
 import pytest
 
-from conftest import relerr
+from conftest import quantise_links, relerr
 from openstaple_gb300 import api, fields as F
 
 pytestmark = pytest.mark.gpu
@@ -107,21 +107,6 @@ def test_mixed_with_generic_phases(lat_factory):
     assert true_residual(o, u, ph, 0.05, x, b, 0.1) <= 1e-10
 
 
-def quantize_links_q16(u):
-    """The 16-bit fixed-point sloppy links as the FP32 kernels see them: the
-    first two rows rounded to FP32, then to multiples of 2^-15 (half to even,
-    clamped to +-32767/32768), the third row rebuilt as conj(row0 x row1)."""
-    re = u.real.astype(np.float32).astype(np.float64)
-    im = u.imag.astype(np.float32).astype(np.float64)
-    q = np.clip(np.rint(re * 32768.0), -32767, 32767) + 1j * np.clip(np.rint(im * 32768.0), -32767, 32767)
-    q = q / 32768.0
-    a, c = q[:, 0], q[:, 1]
-    q[:, 2] = np.conj(np.stack([a[:, 1] * c[:, 2] - a[:, 2] * c[:, 1],
-                                a[:, 2] * c[:, 0] - a[:, 0] * c[:, 2],
-                                a[:, 0] * c[:, 1] - a[:, 1] * c[:, 0]], axis=1))
-    return np.ascontiguousarray(q)
-
-
 @pytest.mark.parametrize("fmt", ["f32", "q16"])
 @pytest.mark.parametrize("im_chem_pot", [0.0, 0.2])
 def test_sloppy_operator(lat_factory, fmt, im_chem_pot):
@@ -145,7 +130,7 @@ def test_sloppy_operator(lat_factory, fmt, im_chem_pot):
         api.set_sloppy_links(prev)
     lat.update_host(out)
     m2 = 0.03 ** 2 + 0.01
-    seen = quantize_links_q16(u) if fmt == "q16" else u
+    seen = quantise_links(u, "q16") if fmt == "q16" else u
     assert relerr(out, o.mdagm(seen, b, ph, m2)) <= 2e-6
     if fmt == "q16":
         assert relerr(out, o.mdagm(u, b, ph, m2)) <= 1e-4

@@ -10,34 +10,11 @@ one, lambda/delta makes the next direction repeat the last one and the
 solve stalls; the Hestenes-Stiefel beta keeps the directions conjugate."""
 import numpy as np
 
+from conftest import quantise_links
 from openstaple_gb300 import fields as F
 
 DIMS = (8, 8, 8, 8)
 MASS = 0.01
-
-
-def quantise_q16(u):
-    """Rows 0-1 rounded to FP32, then to multiples of 2^-15, row 2 rebuilt."""
-    re = np.clip(np.rint(u.real.astype(np.float32).astype(np.float64) * 32768.0), -32767, 32767)
-    im = np.clip(np.rint(u.imag.astype(np.float32).astype(np.float64) * 32768.0), -32767, 32767)
-    q = (re + 1j * im) / 32768.0
-    a, c = q[:, 0], q[:, 1]
-    q[:, 2] = np.conj(np.stack([a[:, 1] * c[:, 2] - a[:, 2] * c[:, 1],
-                                a[:, 2] * c[:, 0] - a[:, 0] * c[:, 2],
-                                a[:, 0] * c[:, 1] - a[:, 1] * c[:, 0]], axis=1))
-    return np.ascontiguousarray(q)
-
-
-def quantise(u, fmt):
-    if fmt == "q16":
-        return quantise_q16(u)
-    dt = {"f32": np.float32, "f16": np.float16}[fmt]
-    q = u.real.astype(dt).astype(np.float64) + 1j * u.imag.astype(dt).astype(np.float64)
-    a, c = q[:, 0], q[:, 1]
-    q[:, 2] = np.conj(np.stack([a[:, 1] * c[:, 2] - a[:, 2] * c[:, 1],
-                                a[:, 2] * c[:, 0] - a[:, 0] * c[:, 2],
-                                a[:, 0] * c[:, 1] - a[:, 1] * c[:, 0]], axis=1))
-    return np.ascontiguousarray(q)
 
 
 def mixed_cg_model(o, u, ph, b, every, hestenes_stiefel, max_iter, fmt="q16", delta_frac=None):
@@ -46,7 +23,7 @@ def mixed_cg_model(o, u, ph, b, every, hestenes_stiefel, max_iter, fmt="q16", de
     |r|^2 < delta_frac * max|r|^2 since the last one; returns (iterations,
     FP64 true relative residual)."""
     m2 = MASS * MASS
-    uq = quantise(u, fmt)
+    uq = quantise_links(u, fmt)
     a32 = lambda v: o.mdagm(uq, np.ascontiguousarray(v.astype(np.complex128)), ph, m2).astype(np.complex64)
     a64 = lambda v: o.mdagm(u, np.ascontiguousarray(v), ph, m2)
     dot = lambda x, y: float(np.sum(x.real.astype(np.float64) * y.real + x.imag.astype(np.float64) * y.imag))
