@@ -224,13 +224,15 @@ double real_scal_prod_global(const vec3_soa *in_vect1, const vec3_soa *in_vect2)
 double l2norm2_global(const vec3_soa *in_vect1);                                  /* :42 */
 /* real_scal_prod_global without any device allocation: its scratch (block
  * partials, ticket counter, result) is a fixed 33,920-byte static device
- * array, so it can be called where cudaMalloc cannot (while another thread
- * holds a global-mode stream capture, in loops that must not synchronise the
- * device, or under a fixed device-memory budget).  Limit: 3*sizeh <= 8,388,608
- * complex numbers; larger lattices get an error and NAN.  The first call on a
- * device looks up the array's address and should come before any stream
- * capture; calls that overlap on the GPU share the array and race.  No
- * counterpart in the reference. */
+ * array, so it can be called where cudaMalloc cannot (in loops that must not
+ * take cudaMalloc's implicit device synchronisation, or under a fixed
+ * device-memory budget that forbids further allocations).  Limit: 3*sizeh <=
+ * 8,388,608 complex numbers (sizeh <= 2,796,202); larger lattices get error
+ * -14 and NAN.  The first call on a device looks up the array's address with
+ * that device current, and should come before any stream capture.  Every
+ * call shares the array: calls that overlap on the GPU race.  A NAN return
+ * means this call failed (the error word says why).  No counterpart in the
+ * reference. */
 double ostaple_real_scal_prod_global_noalloc(const vec3_soa *in_vect1, const vec3_soa *in_vect2);
 void combine_in1xfactor_plus_in2(const vec3_soa *in_vect1, const double factor,
                                  const vec3_soa *in_vect2, vec3_soa *out);        /* :48 */

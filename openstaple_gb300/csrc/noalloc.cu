@@ -1,16 +1,15 @@
 // noalloc.cu -- an allocation-free variant of real_scal_prod_global.
 //
 // Some callers cannot allocate device memory at the moment they need a
-// global reduction: a host thread while another thread of the process has a
-// CUDA stream capture open in global mode (cudaMalloc and cudaFree are then
-// illegal), code that must not pay the implicit device synchronisation of
-// cudaMalloc/cudaFree inside a latency-critical loop, and processes that run
-// under a fixed device-memory budget (an MPS client with a memory limit, or a
-// host program that has already divided HBM among its own pools).  For them
-// this entry point keeps its scratch -- the per-block partial sums, the
-// ticket counter and the result slot -- in one file-scope device array of
-// fixed size that every GPU loading the library holds until the process
-// exits.
+// global reduction: code that must not pay the implicit device
+// synchronisation of cudaMalloc/cudaFree inside a latency-critical loop, and
+// processes that run under a fixed device-memory budget (an MPS client with a
+// memory limit, or a host program that has already divided HBM among its own
+// pools and forbids further raw allocations).  For them this entry point
+// keeps its scratch -- the per-block partial sums, the ticket counter and the
+// result slot -- in one file-scope device array of fixed size that every GPU
+// loading the library holds until the process exits.  Lattices with
+// 3*sizeh > 8,388,608 complex numbers are rejected with error -14.
 #include <cstdio>
 #include "reduce.cuh"
 #include "runtime.cuh"
@@ -75,8 +74,12 @@ extern "C" double ostaple_real_scal_prod_global_noalloc(const vec3_soa* in_vect1
   // device address of the static scratch, looked up once per device with that
   // device current (the first call on a device does this set-up)
   static double* s_addr[64] = {nullptr};
-  int devid = 0;
-  OST_CUDA(cudaGetDevice(&devid));
+  int devid = -1;
+  if (cudaGetDevice(&devid) != cudaSuccess) {
+    cudaGetLastError();
+    set_error(-14, "ostaple_real_scal_prod_global_noalloc: no current CUDA device");
+    return NAN;
+  }
   if (devid < 0 || devid >= 64) {
     set_error(-14, "ostaple_real_scal_prod_global_noalloc: device id %d out of range", devid);
     return NAN;
@@ -95,15 +98,28 @@ extern "C" double ostaple_real_scal_prod_global_noalloc(const vec3_soa* in_vect1
   double* scratch = s_addr[devid];
   const double2* a = dev(reinterpret_cast<const double2*>(in_vect1), "in_vect1");
   const double2* b = dev(reinterpret_cast<const double2*>(in_vect2), "in_vect2");
-  if (!a || !b) return NAN;
+  if (!a || !b) return NAN;  // pointer neither registered nor device memory (error recorded)
   cudaStream_t st = rt().stream;
-  // the array keeps the previous call's contents: the ticket counters must start at zero
-  OST_CUDA(cudaMemsetAsync(scratch, 0, NOALLOC_RESULT * sizeof(double), st));
-  const int grid = int((n + NOALLOC_PER_BLOCK - 1) / NOALLOC_PER_BLOCK);
-  k_rdot_noalloc<<<grid, NOALLOC_THREADS, 0, st>>>(a, b, n, scratch);
-  OST_LAUNCH_CHECK();
+  // This call's own CUDA status decides the result: the library's error word
+  // keeps the first failure of any earlier call, so it cannot tell whether
+  // this reduction succeeded.
+  // The array keeps the previous call's contents: the ticket counters must
+  // start at zero.
+  cudaError_t e = cudaMemsetAsync(scratch, 0, NOALLOC_RESULT * sizeof(double), st);
+  if (e == cudaSuccess) {
+    const int grid = int((n + NOALLOC_PER_BLOCK - 1) / NOALLOC_PER_BLOCK);
+    k_rdot_noalloc<<<grid, NOALLOC_THREADS, 0, st>>>(a, b, n, scratch);
+    ++g_kernel_launches;
+    e = cudaGetLastError();
+  }
   double h = NAN;
-  OST_CUDA(cudaMemcpyAsync(&h, scratch + NOALLOC_RESULT, sizeof(double), cudaMemcpyDeviceToHost, st));
-  OST_CUDA(cudaStreamSynchronize(st));
-  return error_code() ? NAN : h;
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(&h, scratch + NOALLOC_RESULT, sizeof(double), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    set_error(int(e), "ostaple_real_scal_prod_global_noalloc: %s", cudaGetErrorString(e));
+    return NAN;
+  }
+  return h;
 }

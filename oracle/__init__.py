@@ -162,6 +162,17 @@ class Oracle:
         self.L.orc_lambda(_p(lam), _p(sp), _p(u), _p(qa))
         return lam
 
+    def sigma(self, lam, u, s, qa, rho):
+        """Sigma from Sigma' (s) and Lambda (compute_sigma, stouting.c:1175-1302)."""
+        out = np.ascontiguousarray(s).copy()
+        self.L.orc_sigma(_p(np.ascontiguousarray(lam)), _p(u), _p(out), _p(np.ascontiguousarray(qa)), rho)
+        return out
+
+    def exp_times_conf(self, u, qa):
+        out = u.copy()
+        self.L.orc_exp_times_conf(_p(u), _p(np.ascontiguousarray(qa)), _p(out))
+        return out
+
     def force_outer(self, u, xs, ph, a):
         a = np.ascontiguousarray(a, dtype=np.float64)
         aux = self.su3()
@@ -217,6 +228,11 @@ class Reference:
         "ref_sigma_prime_to_sigma": (None, [_P, _P, _D]),
         "ref_conf_times_force_ta": (None, [_P, _P, _P]),
         "ref_set_tamat_zero": (None, [_P]),
+        "ref_exp_times_conf": (None, [_P, _P, _P]),
+        "ref_lambda": (None, [_P, _P, _P, _P]),
+        "ref_sigma": (None, [_P, _P, _P, _P, _D]),
+        "ref_stout_wrapper": (None, [_P, _P, _I, _D]),
+        "ref_fermion_force": (None, [_P, _P, _P, _P, _D, _I, _I, _P, _P, _P, _D, _I, _I, _D]),
     }
 
     def __init__(self, dims):
@@ -330,3 +346,37 @@ class Reference:
         out = ipdot.copy()
         self.L.ref_conf_times_force_ta(_p(u), _p(sigma), _p(out))
         return out
+
+    def exp_times_conf(self, u, qa):
+        out = u.copy()
+        self.L.ref_exp_times_conf(_p(u), _p(np.ascontiguousarray(qa)), _p(out))
+        return out
+
+    def lambda_(self, sp, u, qa):
+        lam = self.tamat()
+        self.L.ref_lambda(_p(lam), _p(np.ascontiguousarray(sp)), _p(u), _p(np.ascontiguousarray(qa)))
+        return lam
+
+    def sigma(self, lam, u, s, qa, rho):
+        out = np.ascontiguousarray(s).copy()
+        self.L.ref_sigma(_p(np.ascontiguousarray(lam)), _p(u), _p(out), _p(np.ascontiguousarray(qa)), rho)
+        return out
+
+    def stout_levels(self, u, steps, rho):
+        """stout_wrapper: (steps*8, 3, 3, sizeh) smeared levels (rows 0-1 written)."""
+        lv = np.zeros((8 * steps, 3, 3, self.sizeh), np.complex128)
+        self.L.ref_stout_wrapper(_p(u), _p(lv), steps, rho)
+        return lv
+
+    def fermion_force(self, u, ph, mass, a, b, phis, res, steps=2, rho=0.15, max_cg=10000):
+        """ipdot of fermion_force_soloopenacc for one flavour with len(phis)
+        pseudofermions and approx_md = (a, b)."""
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        phis = np.ascontiguousarray(phis, dtype=np.complex128).reshape(-1, 3, self.sizeh)
+        lv = np.zeros((8 * max(steps, 1), 3, 3, self.sizeh), np.complex128)
+        ip = self.tamat()
+        ph = np.ascontiguousarray(ph)
+        self.L.ref_fermion_force(_p(u), _p(lv), _p(ip), _p(ph), mass, len(phis), len(a), _p(a), _p(b), _p(phis),
+                                 res, max_cg, steps, rho)
+        return ip

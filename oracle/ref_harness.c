@@ -70,9 +70,20 @@ double calc_diff_force_norm(const tamat_soa *a, const tamat_soa *b) { return 0.0
 void copy_ipdot_into_old(const tamat_soa *a, tamat_soa *b) {}
 void dbg_print_su3_soa(su3_soa *const conf, const char *n, int i) {}
 void convert_double_to_float_su3_soa(const su3_soa *d, su3_soa_f *f) {}
+
+/* The double-precision branch of the reference's inverter_multishift_wrapper
+ * (inverter_wrappers.c:41-114 with singlePInvAccelMultiInv = 0): one call of
+ * the reference's multishift_invert with the package's work vectors.
+ * inverter_wrappers.c itself is not compiled here because it needs the
+ * generated single-precision sources. */
 int inverter_multishift_wrapper(inverter_package ip, ferm_param *pars, RationalApprox *approx,
                                 vec3_soa *out, const vec3_soa *in, double res, int max_cg, int ci)
-{ return 0; }
+{
+  int cg = 0;
+  multishift_invert(ip.u, pars, approx, out, in, res, ip.loc_r, ip.loc_h, ip.loc_s, ip.loc_p,
+                    ip.ferm_shift_temp, max_cg, &cg);
+  return cg;
+}
 
 static void *xalloc(size_t n)
 {
@@ -280,3 +291,85 @@ void ref_conf_times_force_ta(const double *u, const double *auxmat, double *ipdo
 }
 
 void ref_set_tamat_zero(double *t) { set_tamat_soa_to_zero((tamat_soa *)t); }
+
+/* ---- stout chain pieces, one by one (stouting.c:136-165, 516-546, 1175-1302) ---- */
+void ref_exp_times_conf(const double *u, const double *qa, double *uout)
+{
+  su3_soa *aux = xalloc(8 * sizeof(su3_soa));
+  exp_minus_QA_times_conf((const su3_soa *)u, (const tamat_soa *)qa, (su3_soa *)uout, aux);
+  free(aux);
+}
+
+void ref_lambda(double *lam, const double *sp, const double *u, const double *qa)
+{
+  su3_soa *tmp = xalloc(8 * sizeof(su3_soa));
+  compute_lambda((thmat_soa *)lam, (const su3_soa *)sp, (const su3_soa *)u, (const tamat_soa *)qa, tmp);
+  free(tmp);
+}
+
+void ref_sigma(const double *lam, const double *u, double *s, const double *qa, double rho)
+{
+  gl_stout_rho = rho;
+  su3_soa *tmp = xalloc(8 * sizeof(su3_soa));
+  compute_sigma((const thmat_soa *)lam, (const su3_soa *)u, (su3_soa *)s, (const tamat_soa *)qa, tmp, 0);
+  free(tmp);
+}
+
+/* the parking globals stout_wrapper works in (alloc_vars.c) */
+static void stout_globals(int alloc)
+{
+  if (alloc) {
+    auxbis_conf_acc = xalloc(8 * sizeof(su3_soa));
+    glocal_staples = xalloc(8 * sizeof(su3_soa));
+    gipdot = xalloc(8 * sizeof(tamat_soa));
+  } else {
+    free(auxbis_conf_acc); free(glocal_staples); free(gipdot);
+    auxbis_conf_acc = glocal_staples = NULL; gipdot = NULL;
+  }
+}
+
+/* act_params.stout_steps levels of stout smearing (stouting.c:27-72) */
+void ref_stout_wrapper(const double *u, double *levels, int steps, double rho)
+{
+  act_params.stout_steps = steps;
+  gl_stout_rho = rho;
+  stout_globals(1);
+  stout_wrapper((const su3_soa *)u, (su3_soa *)levels, 0);
+  stout_globals(0);
+}
+
+/* The whole rational fermion force of one flavour through the stout levels,
+ * by the reference's own fermion_force_soloopenacc (fermion_force.c:166-320):
+ * nps pseudofermions phi[nps], the approximation (order, a, b) as approx_md,
+ * multi-shift solves to res.  ipdot receives the force (tamat_soa[8]). */
+void ref_fermion_force(const double *u, double *levels, double *ipdot, double *ph, double mass, int nps,
+                       int order, const double *a, const double *b, const double *phi, double res,
+                       int max_cg, int steps, double rho)
+{
+  size_t vb = sizeof(vec3_soa);
+  act_params.stout_steps = steps;
+  gl_stout_rho = rho;
+  aux_th = xalloc(8 * sizeof(thmat_soa));
+  aux_ta = xalloc(8 * sizeof(tamat_soa));
+  stout_globals(1);
+  su3_soa *gl3 = xalloc(8 * sizeof(su3_soa)), *taux = xalloc(8 * sizeof(su3_soa));
+  vec3_soa *shiftmulti = xalloc(vb * (size_t)order), *shifttemp = xalloc(vb * (size_t)order);
+  vec3_soa *r = xalloc(vb), *h = xalloc(vb), *s = xalloc(vb), *p = xalloc(vb);
+  ferm_param fp; make_fp(&fp, ph, mass);
+  fp.number_of_ps = nps;
+  fp.index_of_the_first_ps = 0;
+  fp.approx_md.approx_order = order;
+  for (int i = 0; i < order; i++) { fp.approx_md.RA_a[i] = a[i]; fp.approx_md.RA_b[i] = b[i]; }
+  inverter_package ip;
+  memset(&ip, 0, sizeof(ip));
+  ip.u = (const su3_soa *)u;
+  ip.ferm_shift_temp = shifttemp; ip.nshifts = order;
+  ip.loc_r = r; ip.loc_h = h; ip.loc_s = s; ip.loc_p = p;
+  fermion_force_soloopenacc((su3_soa *)u, (su3_soa *)levels, gl3, (tamat_soa *)ipdot, &fp, 1,
+                            (const vec3_soa *)phi, res, taux, shiftmulti, ip, max_cg);
+  free(gl3); free(taux); free(shiftmulti); free(shifttemp);
+  free(r); free(h); free(s); free(p);
+  free(aux_th); free(aux_ta);
+  aux_th = NULL; aux_ta = NULL;
+  stout_globals(0);
+}

@@ -67,3 +67,27 @@ def quantise_links(u, fmt):
 
 def load_golden(tag: str):
     return dict(np.load(GOLDEN / f"dirac_{tag}.npz"))
+
+
+def load_gauge_fixture(tag: str):
+    """(fixture, dims, links, Sigma', shift solutions X_k, pseudofermions)
+    of tests/golden/gauge_<tag>.npz, the inputs regenerated from their seeds
+    and checked against the stored checksums."""
+    sys.path.insert(0, str(GOLDEN))
+    import make_golden as mg
+    g = dict(np.load(GOLDEN / f"gauge_{tag}.npz"))
+    dims = tuple(int(d) for d in g["dims"])
+    u, sig, xs, phis = mg.gauge_inputs(dims, int(g["link_seed"]), float(g["eps"]))
+    for name, arr in (("u", u), ("sig", sig), ("xs", xs), ("phi", phis)):
+        assert np.isclose(np.sum(np.abs(arr) ** 2), float(g[f"{name}_checksum"]), rtol=1e-14), name
+    return g, dims, u, sig, xs, phis
+
+
+def sample_sites(f, g):
+    """su3/vec3 field at the fixture's sampled half-lattice sites."""
+    return np.asarray(f)[..., g["sites"]]
+
+
+def sample_alg(f, g):
+    """tamat/thmat field (8, 8*sizeh) at the fixture's sampled sites."""
+    return np.asarray(f)[:, g["alg_idx"]]

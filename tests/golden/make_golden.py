@@ -3,9 +3,19 @@ compiled C code (oracle/_ref, built by oracle/Makefile.ref from the reference
 source tree) and copies the coefficients of the two rational approximations
 used by the benchmark configurations out of the reference's .REMEZ files.
 
-Run from the repository root where the reference source tree is available:
+Run from the repository root where the reference source tree is available
+(its path as the first argument, or in OSTAPLE_REFERENCE), optionally naming
+the fixture groups to write (default: all):
 
-    python tests/golden/make_golden.py [/path/to/reference]
+    python tests/golden/make_golden.py /path/to/reference [dirac] [gauge] [config2]
+
+* dirac   -- dirac_<dims>.npz: D_eo/D_oe, M^+M, CG, CG-M, eigenvalue bounds;
+* gauge   -- gauge_<dims>_e<eps>.npz: staples, Q_A, stout levels,
+  exp(-Q_A)U, Lambda, Sigma, the force outer products, the backfield and TA
+  steps and a whole fermion_force_soloopenacc with two pseudofermions;
+* config2 -- config2_16x16x16x16.npz: the 16^4 benchmark configuration
+  (2 stout steps of rho = 0.15, m = 0.05, order-8 CG-M to 1e-10 per shift,
+  the rational fermion force), at sampled sites.
 
 Inputs are regenerated from seeds by openstaple_gb300.fields, whose
 counter-based generator is platform independent; the fixture also stores a
@@ -14,6 +24,7 @@ checksum of every input so a test can detect a generator change.
 from __future__ import annotations
 
 import json
+import os
 import re
 import sys
 from pathlib import Path
@@ -57,11 +68,17 @@ def checksum(x: np.ndarray) -> float:
     return float(np.sum(np.abs(x.astype(np.complex128)) ** 2))
 
 
-def main(refroot: str) -> None:
-    ref = Path(refroot)
-    approx = {k: parse_remez(ref / v) for k, v in APPROX_FILES.items()}
-    (HERE / "ratapprox.json").write_text(json.dumps(approx, indent=1))
+def approx_rescaled(approx: dict, key: str, lam_max: float = 64.0):
+    """(a0, a, b) of a mother approximation on [lambda_min, 1] rescaled as
+    rescale_rational_approximation() does for lambda_max (rationalapprox.c:
+    145-194): scale = 1.05 * lambda_max."""
+    ap = approx[key]
+    mx = lam_max * 1.05
+    eps = mx ** (ap["exponent_num"] / ap["exponent_den"])
+    return ap["a0"] * eps, np.array(ap["a"]) * mx * eps, np.array(ap["b"]) * mx
 
+
+def write_dirac(approx: dict) -> None:
     build.build_reference_oracles([c[0] for c in CASES])
     for dims, sl, ss, mass in CASES:
         r = Reference(dims)
@@ -76,14 +93,7 @@ def main(refroot: str) -> None:
         out["mdagm_shift"] = r.mdagm(u, v, ph, mass, 0.37)
         st, n, x = r.cg(u, ph, mass, v, 1e-10, 10000, 0.0, 10000)
         out.update(cg_status=st, cg_iters=n, cg_x=x)
-        ap = approx["order8"]
-        # rescaled as rescale_rational_approximation() does for lambda_max = 64
-        # (rationalapprox.c:145-194): scale = 1.05 * max
-        mx = 64.0 * 1.05
-        eps = mx ** (ap["exponent_num"] / ap["exponent_den"])
-        a0 = ap["a0"] * eps
-        a = np.array(ap["a"]) * mx * eps
-        b = np.array(ap["b"]) * mx
+        a0, a, b = approx_rescaled(approx, "order8")
         st, n, xs = r.cgm(u, ph, mass, a0, a, b, v, 1e-10, 10000)
         out.update(cgm_status=st, cgm_iters=n, cgm_xs=xs, cgm_recombined=r.recombine(xs, v, a0, a))
         # eigenvalue bounds (find_min_max.c:21-117) from the source as start vector
@@ -95,5 +105,133 @@ def main(refroot: str) -> None:
         print("wrote", tag, "cg", out["cg_iters"], "cgm", out["cgm_iters"], "eig", mm, mn)
 
 
+# (dims, link seed, link eps, sampling stride): eps = 0.01 keeps every c1 of
+# the Cayley-Hamilton exponential below 4e-3 (the series branch)
+GAUGE_CASES = [((4, 4, 4, 4), 101, 0.3, 1), ((4, 4, 4, 4), 102, 0.01, 2), ((4, 6, 8, 10), 103, 0.05, 15)]
+GAUGE_RHO = 0.15
+SIGMA_SEED, XS_SEED, PHI_SEED, FORCE_MASS = 18, 40, 52, 0.1
+
+
+def gauge_inputs(dims, link_seed, eps):
+    """The inputs of a gauge fixture, regenerated from seeds: links, a
+    Sigma' field, four shift solutions X_k, two pseudofermions."""
+    u = F.random_su3_links(dims, link_seed, eps=eps)
+    sig = F.random_su3_links(dims, SIGMA_SEED, eps=1.0) * 0.7
+    xs = np.stack([F.gaussian_vec3(dims, XS_SEED + k) for k in range(4)])
+    phis = np.stack([F.gaussian_vec3(dims, PHI_SEED + k) for k in range(2)])
+    return u, sig, xs, phis
+
+
+FORCE_A = [0.31, 0.21, 0.11, 0.07]
+
+
+def alg_index(sh: int, sites: np.ndarray) -> np.ndarray:
+    """Indices, within one direction of a tamat_soa/thmat_soa array viewed
+    as 8*sizeh doubles (c01, c02, c12 complex, then two real diagonals;
+    struct_c_def.h:47-60), of the entries that belong to the given sites."""
+    parts = []
+    for k in range(3):
+        parts.append(np.stack([k * 2 * sh + 2 * sites, k * 2 * sh + 2 * sites + 1], axis=1).ravel())
+    for k in range(2):
+        parts.append(6 * sh + k * sh + sites)
+    return np.concatenate(parts)
+
+
+def write_gauge(approx: dict) -> None:
+    build.build_reference_oracles(sorted({c[0] for c in GAUGE_CASES}))
+    a0, a8, b8 = approx_rescaled(approx, "order8")
+    for dims, sl, eps, stride in GAUGE_CASES:
+        r = Reference(dims)
+        ph = r.phases()
+        u, sig, xs, phis = gauge_inputs(dims, sl, eps)
+        sites = np.arange(0, r.sizeh, stride)
+        aidx = alg_index(r.sizeh, sites)
+
+        def smp(f):
+            return np.ascontiguousarray(f[..., sites])
+
+        stap = r.staples(u)
+        qa = r.rho_ta(u, stap, GAUGE_RHO)
+        levels = r.stout_levels(u, 2, GAUGE_RHO)
+        lam = r.lambda_(sig, u, qa)
+        out = dict(dims=np.array(dims), link_seed=sl, eps=eps, rho=GAUGE_RHO, stride=stride, sites=sites, alg_idx=aidx,
+                   u_checksum=checksum(u), sig_checksum=checksum(sig), xs_checksum=checksum(xs),
+                   phi_checksum=checksum(phis), force_mass=FORCE_MASS, force_a=np.array(FORCE_A),
+                   md_a=a8, md_b=b8)
+
+        def smp_alg(f):
+            return np.ascontiguousarray(f[:, aidx])
+
+        out["staples"] = smp(stap)
+        out["qa"] = smp_alg(qa)
+        out["stout1"] = smp(levels[:8, :2])
+        out["stout2"] = smp(levels[8:, :2])
+        out["exp_qa_u"] = smp(r.exp_times_conf(u, qa)[:, :2])
+        out["lambda"] = smp_alg(lam)
+        out["sigma"] = smp(r.sigma(lam, u, sig, qa, GAUGE_RHO))
+        out["sigma_prime_to_sigma"] = smp(r.sigma_prime_to_sigma(sig, u, GAUGE_RHO))
+        aux = r.force_outer(u, xs, ph, FORCE_A)
+        out["force_outer"] = smp(aux)
+        pip = r.backfield_times_force(ph, aux, np.zeros_like(aux))
+        out["backfield"] = smp(pip)
+        out["conf_force_ta"] = smp_alg(r.conf_times_force_ta(u, pip, r.tamat()))
+        out["fermion_force"] = smp_alg(r.fermion_force(u, ph, FORCE_MASS, a8, b8, phis, 1e-12))
+        tag = "x".join(map(str, dims)) + f"_e{eps:g}"
+        np.savez_compressed(HERE / f"gauge_{tag}.npz", **out)
+        print("wrote gauge", tag)
+
+
+# the 16^4 benchmark configuration: seeded exp(0.3 i H) links, 2 stout steps
+# rho = 0.15, m = 0.05, one Gaussian source, order-8 x^(-1/4) to 1e-10 per
+# shift, the rational fermion force; stored at every CONFIG2_STRIDE-th site
+CONFIG2 = dict(dims=(16, 16, 16, 16), link_seed=21, src_seed=22, mass=0.05, rho=0.15, steps=2, res=1e-10)
+CONFIG2_STRIDE = 61
+
+
+def write_config2(approx: dict) -> None:
+    c = CONFIG2
+    dims = c["dims"]
+    build.build_reference_oracles([dims])
+    r = Reference(dims)
+    ph = r.phases()
+    u = F.random_su3_links(dims, c["link_seed"])
+    phi = F.gaussian_vec3(dims, c["src_seed"])
+    a0, a, b = approx_rescaled(approx, "order8")
+    levels = r.stout_levels(u, c["steps"], c["rho"])
+    u2 = np.ascontiguousarray(levels[8:])
+    st, n, xs = r.cgm(u2, ph, c["mass"], a0, a, b, phi, c["res"], 10000)
+    rec = r.recombine(xs, phi, a0, a)
+    ipdot = r.fermion_force(u, ph, c["mass"], a, b, phi[None], c["res"], steps=c["steps"], rho=c["rho"])
+    sites = np.arange(0, r.sizeh, CONFIG2_STRIDE)
+    out = dict(dims=np.array(dims), sites=sites, u_checksum=checksum(u), src_checksum=checksum(phi),
+               a0=a0, a=a, b=b, cgm_status=st, cgm_iters=n,
+               stout2=np.ascontiguousarray(levels[8:, :2][..., sites]),
+               cgm_xs=np.ascontiguousarray(xs[..., sites]), recombined=np.ascontiguousarray(rec[..., sites]),
+               xs_norm2=np.array([checksum(x) for x in xs]),
+               alg_idx=alg_index(r.sizeh, sites),
+               fermion_force=np.ascontiguousarray(ipdot[:, alg_index(r.sizeh, sites)]))
+    out.update({k: v for k, v in c.items() if k not in ("dims",)})
+    np.savez_compressed(HERE / "config2_16x16x16x16.npz", **out)
+    print("wrote config2: cgm", n, "iterations, status", st)
+
+
+def main(refroot: str, groups) -> None:
+    ref = Path(refroot)
+    os.environ["OSTAPLE_REFERENCE"] = str(ref)
+    approx = {k: parse_remez(ref / v) for k, v in APPROX_FILES.items()}
+    (HERE / "ratapprox.json").write_text(json.dumps(approx, indent=1))
+    if "dirac" in groups:
+        write_dirac(approx)
+    if "gauge" in groups:
+        write_gauge(approx)
+    if "config2" in groups:
+        write_config2(approx)
+
+
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    args = sys.argv[1:]
+    root = args.pop(0) if args and not args[0] in ("dirac", "gauge", "config2") else os.environ.get(
+        "OSTAPLE_REFERENCE")
+    if not root:
+        sys.exit("usage: make_golden.py /path/to/reference [dirac] [gauge] [config2]")
+    main(root, set(args) or {"dirac", "gauge", "config2"})

@@ -122,3 +122,153 @@ def test_oracle_cg_max_iterations_failure(built):
     v = F.gaussian_vec3(dims, 4)
     st, n, _ = o.cg(u, ph, 0.1, v, 1e-10, max_cg=5, restart=5)
     assert st == 0 and n == 5
+
+
+# ---- stout smearing and the fermion force chain ---------------------------
+# Tolerances (relative, max-norm): 1e-14 for the staples, Q_A, the stout
+# exponential and the outer products; 5e-14 for Lambda and the Sigma chain,
+# whose Cayley-Hamilton derivative coefficients divide by (9u^2 - w^2)^2;
+# 1e-12 for a whole force, which includes two multi-shift solves to 1e-12.
+
+GAUGE_TAGS = ["4x4x4x4_e0.3", "4x4x4x4_e0.01", "4x6x8x10_e0.05"]
+
+
+from conftest import load_gauge_fixture as _gauge_fixture  # noqa: E402
+from conftest import sample_alg as _smp_alg  # noqa: E402
+from conftest import sample_sites as _smp  # noqa: E402
+
+
+@pytest.mark.parametrize("dims", REF_DIMS)
+@pytest.mark.parametrize("eps", [0.3, 0.01])
+def test_oracle_gauge_chain_matches_compiled_reference(built, dims, eps):
+    """Staples, Q_A, two stout levels, exp(-Q_A) U, Lambda, Sigma, the
+    Sigma' -> Sigma step, the outer products, the backfield and the TA
+    projection: the oracle against the reference's own compiled C
+    (stouting.c:27-1302, plaquettes.c:196-259, fermion_force_utilities.c:
+    30-153).  eps = 0.01 puts every link in the c1 < 4e-3 series branch of
+    the exponential (cayley_hamilton.h:67-72)."""
+    from oracle import Oracle, Reference, ref_available
+    if not ref_available(dims):
+        pytest.skip("reference not compiled here (no reference source tree)")
+    r, o = Reference(dims), Oracle(dims)
+    u = F.random_su3_links(dims, 201, eps=eps)
+    sig = F.random_su3_links(dims, 202, eps=1.0) * 0.7
+    ph = r.phases()
+    stap = r.staples(u)
+    assert relerr(o.staples(u), stap) <= 1e-14
+    qa = r.rho_ta(u, stap, 0.15)
+    assert relerr(o.rho_ta(u, stap, 0.15), qa) <= 1e-14
+    lv = r.stout_levels(u, 2, 0.15)
+    l1 = o.stout(u, 0.15)
+    assert relerr(l1[:, :2], lv[:8, :2]) <= 1e-14
+    assert relerr(o.stout(l1, 0.15)[:, :2], lv[8:, :2]) <= 1e-14
+    assert relerr(o.exp_times_conf(u, qa)[:, :2], r.exp_times_conf(u, qa)[:, :2]) <= 1e-14
+    lam = r.lambda_(sig, u, qa)
+    assert relerr(o.lambda_(sig, u, qa), lam) <= 5e-14
+    assert relerr(o.sigma(lam, u, sig, qa, 0.15), r.sigma(lam, u, sig, qa, 0.15)) <= 5e-14
+    assert relerr(o.sigma_prime_to_sigma(sig, u, 0.15), r.sigma_prime_to_sigma(sig, u, 0.15)) <= 5e-14
+    xs = np.stack([F.gaussian_vec3(dims, 210 + k) for k in range(3)])
+    a = [0.5, 0.25, 0.125]
+    aux = r.force_outer(u, xs, ph, a)
+    assert relerr(o.force_outer(u, xs, ph, a), aux) <= 1e-14
+    pip = r.backfield_times_force(ph, aux, sig)
+    assert relerr(o.backfield_times_force(ph, aux, sig), pip) <= 1e-14
+    t0 = r.tamat()
+    assert relerr(o.conf_times_force_ta(u, pip, t0), r.conf_times_force_ta(u, pip, t0)) <= 1e-14
+
+
+def _oracle_force(o, u, ph, mass, a, b, phis, res, rho=0.15):
+    """The fermion_force_soloopenacc chain (fermion_force.c:166-320) from
+    oracle pieces: two stout levels, one CG-M per pseudofermion with
+    approx_md, outer products, phases, Sigma' -> Sigma per level, -TA(U Sigma)."""
+    u1 = o.stout(u, rho)
+    u2 = o.stout(u1, rho)
+    aux = o.su3()
+    for phi in phis:
+        st, n, xs = o.cgm(u2, ph, mass, b, np.ascontiguousarray(phi), res)
+        assert st == 1
+        aux += o.force_outer(u2, xs, ph, a)
+    sig = o.backfield_times_force(ph, aux, np.zeros_like(aux))
+    sig = o.sigma_prime_to_sigma(sig, u1, rho)
+    sig = o.sigma_prime_to_sigma(sig, u, rho)
+    return o.conf_times_force_ta(u, sig, o.tamat())
+
+
+@pytest.mark.parametrize("dims", [(4, 4, 4, 4), (4, 6, 8, 10)])
+def test_oracle_fermion_force_matches_compiled_reference(built, dims):
+    """A whole fermion_force_soloopenacc (2 stout levels, two pseudofermions,
+    order-8 approx_md) run by the reference's own compiled code against the
+    oracle chain."""
+    import json
+    from conftest import GOLDEN
+    from oracle import Oracle, Reference, ref_available
+    if not ref_available(dims):
+        pytest.skip("reference not compiled here (no reference source tree)")
+    r, o = Reference(dims), Oracle(dims)
+    ap = json.loads((GOLDEN / "ratapprox.json").read_text())["order8"]
+    mx = 64.0 * 1.05
+    e = mx ** (ap["exponent_num"] / ap["exponent_den"])
+    a, b = np.array(ap["a"]) * mx * e, np.array(ap["b"]) * mx
+    u = F.random_su3_links(dims, 221, eps=0.3)
+    ph = r.phases()
+    phis = np.stack([F.gaussian_vec3(dims, 222), F.gaussian_vec3(dims, 223)])
+    ip_r = r.fermion_force(u, ph, 0.1, a, b, phis, 1e-12)
+    assert relerr(_oracle_force(o, u, ph, 0.1, a, b, phis, 1e-12), ip_r) <= 1e-12
+
+
+@pytest.mark.parametrize("tag", GAUGE_TAGS)
+def test_oracle_matches_golden_gauge(built, tag):
+    """The oracle against the gauge fixtures that the compiled reference
+    wrote (tests/golden/make_golden.py), on every machine."""
+    from oracle import Oracle
+    g, dims, u, sig, xs, phis = _gauge_fixture(tag)
+    o = Oracle(dims)
+    ph = o.phases()
+    rho = float(g["rho"])
+    stap = o.staples(u)
+    assert relerr(_smp(stap, g), g["staples"]) <= 1e-14
+    qa = o.rho_ta(u, stap, rho)
+    assert relerr(_smp_alg(qa, g), g["qa"]) <= 1e-14
+    l1 = o.stout(u, rho)
+    assert relerr(_smp(l1[:, :2], g), g["stout1"]) <= 1e-14
+    assert relerr(_smp(o.stout(l1, rho)[:, :2], g), g["stout2"]) <= 1e-14
+    assert relerr(_smp(o.exp_times_conf(u, qa)[:, :2], g), g["exp_qa_u"]) <= 1e-14
+    lam = o.lambda_(sig, u, qa)
+    assert relerr(_smp_alg(lam, g), g["lambda"]) <= 5e-14
+    assert relerr(_smp(o.sigma(lam, u, sig, qa, rho), g), g["sigma"]) <= 5e-14
+    assert relerr(_smp(o.sigma_prime_to_sigma(sig, u, rho), g), g["sigma_prime_to_sigma"]) <= 5e-14
+    aux = o.force_outer(u, xs, ph, g["force_a"])
+    assert relerr(_smp(aux, g), g["force_outer"]) <= 1e-14
+    pip = o.backfield_times_force(ph, aux, np.zeros_like(aux))
+    assert relerr(_smp(pip, g), g["backfield"]) <= 1e-14
+    assert relerr(_smp_alg(o.conf_times_force_ta(u, pip, o.tamat()), g), g["conf_force_ta"]) <= 1e-14
+    ip = _oracle_force(o, u, ph, float(g["force_mass"]), g["md_a"], g["md_b"], phis, 1e-12, rho)
+    assert relerr(_smp_alg(ip, g), g["fermion_force"]) <= 1e-12
+
+
+def test_oracle_matches_golden_config2(built):
+    """The 16^4 benchmark configuration (2 stout steps of rho = 0.15,
+    m = 0.05, order-8 CG-M to 1e-10 per shift, the rational force) against
+    the compiled reference's outputs at sampled sites: same CG-M iteration
+    count, solutions within 1e-12, force within 1e-11."""
+    from conftest import GOLDEN
+    from oracle import Oracle
+    g = dict(np.load(GOLDEN / "config2_16x16x16x16.npz"))
+    dims = tuple(int(d) for d in g["dims"])
+    u = F.random_su3_links(dims, int(g["link_seed"]))
+    phi = F.gaussian_vec3(dims, int(g["src_seed"]))
+    assert np.isclose(np.sum(np.abs(u) ** 2), float(g["u_checksum"]), rtol=1e-14)
+    assert np.isclose(np.sum(np.abs(phi) ** 2), float(g["src_checksum"]), rtol=1e-14)
+    o = Oracle(dims, threads=8)
+    ph = o.phases()
+    rho, mass, res = float(g["rho"]), float(g["mass"]), float(g["res"])
+    u1 = o.stout(u, rho)
+    u2 = o.stout(u1, rho)
+    assert relerr(_smp(u2[:, :2], g), g["stout2"]) <= 1e-14
+    st, n, xs = o.cgm(u2, ph, mass, g["b"], phi, res)
+    assert st == int(g["cgm_status"]) == 1
+    assert n == int(g["cgm_iters"])
+    assert relerr(_smp(xs, g), g["cgm_xs"]) <= 1e-12
+    assert relerr(_smp(o.recombine(xs, phi, float(g["a0"]), g["a"]), g), g["recombined"]) <= 1e-12
+    ip = _oracle_force(o, u, ph, mass, g["a"], g["b"], phi[None], res, rho)
+    assert relerr(_smp_alg(ip, g), g["fermion_force"]) <= 1e-11
