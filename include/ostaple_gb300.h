@@ -259,6 +259,50 @@ void combine_in1_x_fact1_minus_in2_back_into_in2(const vec3_soa *in1, double fac
 void combine_in1_minus_in2_allxfact(const vec3_soa *in1, const vec3_soa *in2, double fact,
                                     vec3_soa *out);                               /* :109 */
 
+/* ---- single-precision twins (the reference's generated sp_*.c files) -----
+ * Same meaning as the FP64 functions above on the float layouts su3_soa_f /
+ * vec3_soa_f / float_soa (struct_c_def.h types with float complex elements,
+ * sp_struct_c_def.h): FP32 links and vectors, FP64 scalars and FP64
+ * accumulation in the global reductions; phases from ferm_param.phases_f.
+ * The reference's benchmark drivers call them (deo_doe_test.c:311-342,
+ * inverter_multishift_test.c:342). */
+void acc_Deo_f(const su3_soa_f *u, vec3_soa_f *out, const vec3_soa_f *in, const float_soa *backfield);
+void acc_Doe_f(const su3_soa_f *u, vec3_soa_f *out, const vec3_soa_f *in, const float_soa *backfield);
+void acc_Deo_unsafe_f(const su3_soa_f *u, vec3_soa_f *out, const vec3_soa_f *in, const float_soa *backfield);
+void acc_Doe_unsafe_f(const su3_soa_f *u, vec3_soa_f *out, const vec3_soa_f *in, const float_soa *backfield);
+/* sp_fermion_matrix.c: the generator turns this file's `double` into `float` */
+void fermion_matrix_multiplication_f(const su3_soa_f *u, vec3_soa_f *out, const vec3_soa_f *in,
+                                     vec3_soa_f *temp1, ferm_param *pars);
+void fermion_matrix_multiplication_shifted_f(const su3_soa_f *u, vec3_soa_f *out, const vec3_soa_f *in,
+                                             vec3_soa_f *temp1, ferm_param *pars, float shift);
+double l2norm2_global_f(const vec3_soa_f *in_vect1);
+double real_scal_prod_global_f(const vec3_soa_f *in_vect1, const vec3_soa_f *in_vect2);
+void set_vec3_soa_to_zero_f(vec3_soa_f *fermion);
+void assign_in_to_out_f(const vec3_soa_f *in_vect1, vec3_soa_f *out);
+void combine_in1xfactor_plus_in2_f(const vec3_soa_f *in_vect1, const double factor, const vec3_soa_f *in_vect2,
+                                   vec3_soa_f *out);
+void combine_add_factor_x_in2_to_in1_f(vec3_soa_f *in1, const vec3_soa_f *in2, double factor);
+void combine_in1xferm_mass_minus_in2_f(const vec3_soa_f *in_vect1, double ferm_mass2, vec3_soa_f *in_vect2);
+void combine_in1_minus_in2_f(const vec3_soa_f *in_vect1, const vec3_soa_f *in_vect2, vec3_soa_f *out);
+void multiply_fermion_x_doublefactor_f(vec3_soa_f *in1, const double factor);
+int ker_invert_openacc_f(const su3_soa_f *u, ferm_param *pars, vec3_soa_f *solution, const vec3_soa_f *in,
+                         double res, vec3_soa_f *loc_r, vec3_soa_f *loc_h, vec3_soa_f *loc_s, vec3_soa_f *loc_p,
+                         const int max_cg, double shift, int *cg_return);
+int multishift_invert_f(const su3_soa_f *u, ferm_param *pars, RationalApprox *approx, vec3_soa_f *out,
+                        const vec3_soa_f *in, double residuo, vec3_soa_f *loc_r, vec3_soa_f *loc_h,
+                        vec3_soa_f *loc_s, vec3_soa_f *loc_p, vec3_soa_f *shiftferm, const int max_cg,
+                        int *cg_return);
+void recombine_shifted_vec3_to_vec3_f(const vec3_soa_f *in_shifted, const vec3_soa_f *in, vec3_soa_f *out,
+                                      const RationalApprox *approx);
+/* float <-> double conversions (float_double_conv.h:13-55): one vec3_soa,
+ * one double_soa, or all 8 directions of a su3_soa (3 rows each) */
+void convert_double_to_float_vec3_soa(const vec3_soa *d_var, vec3_soa_f *f_var);
+void convert_float_to_double_vec3_soa(const vec3_soa_f *f_var, vec3_soa *d_var);
+void convert_double_to_float_real_soa(const double_soa *d_var, float_soa *f_var);
+void convert_float_to_double_real_soa(const float_soa *f_var, double_soa *d_var);
+void convert_double_to_float_su3_soa(const su3_soa *d_var, su3_soa_f *f_var);
+void convert_float_to_double_su3_soa(const su3_soa_f *f_var, su3_soa *d_var);
+
 /* ---- solvers ------------------------------------------------------------ */
 /* CG on (M^+M + shift) x = in, restarted every inverter_tricks.restartingEvery
  * iterations (inverter_full.h:20-31). */
@@ -293,11 +337,11 @@ void recombine_shifted_vec3_to_vec3(const vec3_soa *in_shifted, const vec3_soa *
  * loc_p / loc_p1 holds a Gaussian start vector on entry; the iteration stops
  * when the relative change of |p| is <= 1e-5.  find_min_max sets
  * minmax[0] = m^2 and minmax[1] = the largest eigenvalue. */
-double ker_find_max_eigenvalue_openacc(const su3_soa *u, ferm_param *pars, vec3_soa *loc_r, vec3_soa *loc_h,
+double ker_find_max_eigenvalue_openacc(su3_soa *u, ferm_param *pars, vec3_soa *loc_r, vec3_soa *loc_h,
                                        vec3_soa *loc_p);
-double ker_find_min_eigenvalue_openacc(const su3_soa *u, ferm_param *pars, vec3_soa *loc_r, vec3_soa *loc_h,
+double ker_find_min_eigenvalue_openacc(su3_soa *u, ferm_param *pars, vec3_soa *loc_r, vec3_soa *loc_h,
                                        vec3_soa *loc_p, double max);
-void find_min_max_eigenvalue_soloopenacc(const su3_soa *u, ferm_param *pars, vec3_soa *loc_r, vec3_soa *loc_h,
+void find_min_max_eigenvalue_soloopenacc(su3_soa *u, ferm_param *pars, vec3_soa *loc_r, vec3_soa *loc_h,
                                          vec3_soa *loc_p1, vec3_soa *loc_p2, double *minmax);
 
 /* out = (m^2 + shift) in - D_eo D_oe in computed in double-float arithmetic

@@ -82,4 +82,13 @@ struct CgmBatchResult {
 CgmBatchResult batched_cgm_f32(const CgmBatchBuffers& B, double mass2, const double* shifts, double res,
                                int max_iter, cudaStream_t st);
 
+// All `order` shifts for nrhs <= 4 right-hand sides (device FP64 fields,
+// xs64[r*order + k]): an FP32 CG-M for all right-hand sides together to the
+// relative residual res_cgm, then (refine != 0) every system refined to an
+// FP64 true residual <= res by the batched mixed solver.  Returns
+// INVERTER_SUCCESS / INVERTER_FAILURE (capi_batched.cu).
+int multishift_two_phase(const double2* u64, const double* ph64, double mass, const double* shifts, int order,
+                         int nrhs, const double2* b64, double2* xs64, double res_cgm, double res, int max_iter,
+                         double delta_frac, int refine, int* iters_cgm, int* iters_refine, double* true_res);
+
 }  // namespace ost

@@ -9,6 +9,7 @@
 #include "kernels.cuh"
 #include "runtime.cuh"
 #include "solver_kernels.cuh"
+#include "solvers_fp.cuh"
 #include "../../include/ostaple_gb300.h"
 
 using namespace ost;
@@ -24,7 +25,6 @@ namespace {
 typedef double2 Z;
 
 inline long vlen() { return 3L * rt().g.sizeh; }           // complex numbers in a vec3_soa
-inline long su3len() { return 9L * rt().g.sizeh; }         // complex numbers in a su3_soa
 inline cudaStream_t S() { return rt().stream; }
 
 void dslash64(int parity, const su3_soa* u, vec3_soa* out, const vec3_soa* in, const double_soa* bf,
@@ -45,31 +45,11 @@ void dslash64(int parity, const su3_soa* u, vec3_soa* out, const vec3_soa* in, c
   launch_dslash<double>(a);
 }
 
-// device-side M^+M with the temp field: tmp = D_oe in ; out = m2 in - D_eo tmp
-void mdagm_dev(const Z* u, Z* out, const Z* in, Z* tmp, const void* ph, double m2) {
-  DslashArgs<double> a;
-  a.phase_mode = PH_ANGLE;
-  a.u = u;
-  a.phases = ph;
-  a.stream = S();
-  a.mass2 = 0;
-  a.in0 = nullptr;
-  a.parity = 1; a.epilogue = EPI_PLAIN; a.out = tmp; a.in = in;
-  launch_dslash<double>(a);
-  a.parity = 0; a.epilogue = EPI_MDAGM; a.out = out; a.in = tmp; a.in0 = in; a.mass2 = m2;
-  launch_dslash<double>(a);
-}
+using fp::dscal;
+using fp::readback;
 
-// one-double device scalar slots read back by the host solvers
-double* dscal(int k) {
-  double* p = static_cast<double*>(workspace(WS_SCALARS, 64 * sizeof(double)));
-  return p ? p + k : nullptr;
-}
-double readback(const double* d) {
-  double h = 0;
-  OST_CUDA(cudaMemcpyAsync(&h, d, sizeof(double), cudaMemcpyDeviceToHost, S()));
-  OST_CUDA(cudaStreamSynchronize(S()));
-  return h;
+inline void mdagm_dev(const Z* u, Z* out, const Z* in, Z* tmp, const void* ph, double m2) {
+  fp::mdagm<double>(u, out, in, tmp, ph, m2);
 }
 
 }  // namespace
@@ -202,25 +182,42 @@ void set_vec3_soa_to_zero(vec3_soa* f) {
 void multiple_combine_in1_minus_in2x_factor_back_into_in1(vec3_soa* out, const vec3_soa* in, const int maxiter,
                                                           const int* flag, const double* omegas) {
   if (!require_init("multiple_combine_in1_minus_in2x_factor_back_into_in1")) return;
+  if (maxiter < 0 || maxiter > OST_MAX_SHIFTS) {
+    set_error(-11, "multiple_combine_in1_minus_in2x_factor_back_into_in1: maxiter %d outside [0,%d]", maxiter,
+              OST_MAX_SHIFTS);
+    return;
+  }
   Z* o = DVW(out, "out");
   const Z* a = DV(in, "in");
-  if (!o || !a) return;
-  for (int k = 0; k < maxiter; ++k)
-    if (flag[k] == 1) blas_axpy<double>(a + k * vlen(), -omegas[k], o + k * vlen(), o + k * vlen(), vlen(), S());
+  if (!o || !a || maxiter == 0) return;
+  CgmCoeffs cf{};
+  cf.nshift = maxiter;
+  for (int k = 0; k < maxiter; ++k) {
+    cf.active[k] = flag[k] == 1;
+    cf.omega[k] = omegas[k];
+  }
+  multi_xupdate<double>(o, a, vlen(), cf, vlen(), S());   // out_k -= omegas_k in_k, one pass
 }
 void multiple1_combine_in1_x_fact1_plus_in2_x_fact2_back_into_in1(vec3_soa* in1, int maxiter, const int* flag,
                                                                   const double* gammas, const vec3_soa* in2,
                                                                   const double* zeta_iii) {
   if (!require_init("multiple1_combine_in1_x_fact1_plus_in2_x_fact2_back_into_in1")) return;
+  if (maxiter < 0 || maxiter > OST_MAX_SHIFTS) {
+    set_error(-11, "multiple1_combine_in1_x_fact1_plus_in2_x_fact2_back_into_in1: maxiter %d outside [0,%d]",
+              maxiter, OST_MAX_SHIFTS);
+    return;
+  }
   Z* a = DVW(in1, "in1");
   const Z* b = DV(in2, "in2");
-  if (!a || !b) return;
+  if (!a || !b || maxiter == 0) return;
+  CgmCoeffs cf{};
+  cf.nshift = maxiter;
   for (int k = 0; k < maxiter; ++k) {
-    if (flag[k] != 1) continue;
-    // in1_k = gammas_k in1_k + zeta_k in2
-    blas_scale<double>(a + k * vlen(), gammas[k], vlen(), S());
-    blas_axpy<double>(b, zeta_iii[k], a + k * vlen(), a + k * vlen(), vlen(), S());
+    cf.active[k] = flag[k] == 1;
+    cf.gamma[k] = gammas[k];
+    cf.zeta[k] = zeta_iii[k];
   }
+  multi_pupdate<double>(a, b, vlen(), cf, vlen(), S());   // in1_k = gammas_k in1_k + zeta_k in2, one pass
 }
 void combine_in1_x_fact1_minus_in2_back_into_in2(const vec3_soa* in1, double f, vec3_soa* in2) {
   if (!require_init("combine_in1_x_fact1_minus_in2_back_into_in2")) return;
@@ -246,50 +243,8 @@ int ker_invert_openacc(const su3_soa* u, ferm_param* pars, vec3_soa* solution, c
   Z *r = DVW(loc_r, "loc_r"), *h = DVW(loc_h, "loc_h"), *s = DVW(loc_s, "loc_s"), *p = DVW(loc_p, "loc_p");
   const void* ph = resolve(pars->phases, "phases");
   if (!du || !x || !b || !r || !h || !s || !p || !ph) return INVERTER_FAILURE;
-  const long n = vlen();
-  const double m2 = pars->ferm_mass * pars->ferm_mass + shift;
-  const double SAFETY = 0.95;
-  const int restart = inverter_tricks.restartingEvery > 0 ? inverter_tricks.restartingEvery : 10000;
-
-  blas_norm2<double>(b, n, dscal(0), S());
-  const double source_norm = readback(dscal(0));
-  int cg = 0;
-  double delta, alpha, lambda = 0, omega, gammag;
-  do {
-    mdagm_dev(du, s, x, h, ph, m2);
-    blas_axmy<double>(b, 1.0, s, r, n, S());      // r = in - s
-    blas_copy<double>(r, p, n, S());
-    blas_norm2<double>(r, n, dscal(0), S());
-    delta = readback(dscal(0));
-    int cg_restarted = 0;
-    do {
-      cg++;
-      cg_restarted++;
-      mdagm_dev(du, s, p, h, ph, m2);
-      blas_rdot<double>(p, s, n, dscal(1), S());
-      alpha = readback(dscal(1));
-      omega = delta / alpha;
-      blas_axpy<double>(p, omega, x, x, n, S());    // x += omega p
-      fused_axpy_norm<double>(r, s, -omega, n, dscal(2), S());  // r -= omega s ; lambda
-      lambda = readback(dscal(2));
-      gammag = lambda / delta;
-      delta = lambda;
-      blas_axpy<double>(p, gammag, r, p, n, S());   // p = r + gammag p
-      if (error_code()) return INVERTER_FAILURE;
-    } while (std::sqrt(lambda / source_norm) > res * SAFETY && cg_restarted < restart);
-  } while (std::sqrt(lambda / source_norm) > res && cg < max_cg);
-
-  mdagm_dev(du, s, x, h, ph, m2);
-  blas_axmy<double>(b, 1.0, s, h, n, S());
-  blas_norm2<double>(h, n, dscal(3), S());
-  const double current_res = readback(dscal(3)) / source_norm;
-  if (verbosity_lv > 1)
-    printf("Terminated invert after   %d    iterations[res/stop_res=  %e , stop_res=%e ]\n", cg,
-           std::sqrt(current_res) / res, res);
-  if (cg == max_cg) printf("WARNING: maximum number of iterations reached in invert\n");
-  *cg_return = cg;
-  if (error_code()) return INVERTER_FAILURE;
-  return std::sqrt(current_res) <= res ? INVERTER_SUCCESS : INVERTER_FAILURE;
+  return fp::cg<double>(du, ph, pars->ferm_mass, x, b, res, r, h, s, p, max_cg, shift,
+                         inverter_tricks.restartingEvery, cg_return);
 }
 
 // ---- multi-shift CG (inverter_multishift_full.c:23-252) ----
@@ -309,88 +264,8 @@ int multishift_invert(const su3_soa* u, ferm_param* pars, RationalApprox* approx
   Z* ps = DVW(shiftferm, "shiftferm");
   const void* ph = resolve(pars->phases, "phases");
   if (!du || !xs || !b || !r || !h || !s || !p || !ps || !ph) return INVERTER_FAILURE;
-  const long n = vlen();
-  const double m2 = pars->ferm_mass * pars->ferm_mass;
-  const double SAFETY = 0.95;
-
-  double zeta_i[OST_MAX_SHIFTS], zeta_ii[OST_MAX_SHIFTS], zeta_iii[OST_MAX_SHIFTS];
-  double omegas[OST_MAX_SHIFTS], gammas[OST_MAX_SHIFTS];
-  int flag[OST_MAX_SHIFTS];
-  for (int k = 0; k < order; ++k) {
-    flag[k] = 1;
-    blas_zero<double>(xs + k * n, n, S());
-  }
-  blas_copy<double>(b, r, n, S());
-  blas_copy<double>(r, p, n, S());
-  blas_norm2<double>(r, n, dscal(0), S());
-  double delta = readback(dscal(0));
-  blas_norm2<double>(b, n, dscal(1), S());
-  const double source_norm = readback(dscal(1));
-  double omega = 1.0, omega_save, alpha, lambda, gammag = 0.0;
-  for (int k = 0; k < order; ++k) {
-    blas_copy<double>(b, ps + k * n, n, S());
-    zeta_i[k] = 1.0;
-    zeta_ii[k] = 1.0;
-    gammas[k] = 0.0;
-  }
-  int cg = 0;
-  int maxiter = order;
-  do {
-    cg++;
-    mdagm_dev(du, s, p, h, ph, m2);
-    blas_rdot<double>(p, s, n, dscal(2), S());
-    alpha = readback(dscal(2));
-    omega_save = omega;
-    omega = -delta / alpha;
-    for (int k = 0; k < maxiter; ++k) {
-      if (flag[k] == 1) {
-        zeta_iii[k] = (zeta_i[k] * zeta_ii[k] * omega_save) /
-                      (omega * gammag * (zeta_i[k] - zeta_ii[k]) +
-                       zeta_i[k] * omega_save * (1.0 - (approx->RA_b[k]) * omega));
-        omegas[k] = omega * zeta_iii[k] / zeta_ii[k];
-      }
-    }
-    fused_axpy_norm<double>(r, s, omega, n, dscal(3), S());   // r += omega s ; lambda
-    lambda = readback(dscal(3));
-    gammag = lambda / delta;
-    for (int k = 0; k < order; ++k)
-      if (flag[k] == 1) gammas[k] = gammag * zeta_iii[k] * omegas[k] / (zeta_ii[k] * omega);
-    CgmCoeffs cf;
-    cf.nshift = maxiter;
-    for (int k = 0; k < maxiter; ++k) {
-      cf.active[k] = flag[k] == 1;
-      cf.omega[k] = omegas[k];
-      cf.gamma[k] = gammas[k];
-      cf.zeta[k] = zeta_iii[k];
-    }
-    // p = r + gammag p ; x_k -= omegas_k ps_k ; ps_k = gammas_k ps_k + zeta_k r
-    fused_cgm_update<double>(p, r, gammag, xs, ps, n, cf, n, S());
-    maxiter = 0;
-    for (int k = 0; k < order; ++k) {
-      if (flag[k] == 1) {
-        double fact = std::sqrt(delta * zeta_ii[k] * zeta_ii[k] / source_norm);
-        if (fact < residuo * SAFETY) flag[k] = 0;
-        else maxiter = k + 1;
-        zeta_i[k] = zeta_ii[k];
-        zeta_ii[k] = zeta_iii[k];
-      }
-    }
-    delta = lambda;
-    if (error_code()) return INVERTER_FAILURE;
-  } while (maxiter > 0 && cg < max_cg);
-  if (cg == max_cg) printf("WARNING: maximum number of iterations reached in invert\n");
-
-  int check = 1;
-  for (int k = 0; k < order; ++k) {
-    mdagm_dev(du, s, xs + k * n, h, ph, m2 + approx->RA_b[k]);
-    blas_axmy<double>(b, 1.0, s, h, n, S());
-    blas_norm2<double>(h, n, dscal(4), S());
-    double rr = readback(dscal(4)) / source_norm;
-    check *= (rr <= 1) ? 1 : 0;
-  }
-  *cg_return = cg;
-  if (error_code()) return INVERTER_FAILURE;
-  return check ? INVERTER_SUCCESS : INVERTER_FAILURE;
+  return fp::cgm<double>(du, ph, pars->ferm_mass, approx->RA_b, order, xs, b, residuo, r, h, s, p, ps, max_cg,
+                          cg_return);
 }
 
 void recombine_shifted_vec3_to_vec3(const vec3_soa* in_shifted, const vec3_soa* in, vec3_soa* out,
@@ -447,7 +322,7 @@ static double power_iteration(const char* who, const su3_soa* u, ferm_param* par
   return norm;
 }
 
-double ker_find_max_eigenvalue_openacc(const su3_soa* u, ferm_param* pars, vec3_soa* loc_r, vec3_soa* loc_h,
+double ker_find_max_eigenvalue_openacc(su3_soa* u, ferm_param* pars, vec3_soa* loc_r, vec3_soa* loc_h,
                                        vec3_soa* loc_p) {
   return power_iteration("ker_find_max_eigenvalue_openacc", u, pars, 0.0, loc_r, loc_h, loc_p);
 }
@@ -455,14 +330,14 @@ double ker_find_max_eigenvalue_openacc(const su3_soa* u, ferm_param* pars, vec3_
 // The reference passes shift = (max - m^2) - m^2 to the shifted matrix and
 // returns max - |p| (find_min_max.c:62-92); kept as it is.  Its caller does
 // not use it: the minimum is set to m^2.
-double ker_find_min_eigenvalue_openacc(const su3_soa* u, ferm_param* pars, vec3_soa* loc_r, vec3_soa* loc_h,
+double ker_find_min_eigenvalue_openacc(su3_soa* u, ferm_param* pars, vec3_soa* loc_r, vec3_soa* loc_h,
                                        vec3_soa* loc_p, double max) {
   const double m2 = pars->ferm_mass * pars->ferm_mass;
   const double delta = max - m2;
   return max - power_iteration("ker_find_min_eigenvalue_openacc", u, pars, delta - m2, loc_r, loc_h, loc_p);
 }
 
-void find_min_max_eigenvalue_soloopenacc(const su3_soa* u, ferm_param* pars, vec3_soa* loc_r, vec3_soa* loc_h,
+void find_min_max_eigenvalue_soloopenacc(su3_soa* u, ferm_param* pars, vec3_soa* loc_r, vec3_soa* loc_h,
                                          vec3_soa* loc_p1, vec3_soa* loc_p2, double* minmax) {
   (void)loc_p2;
   minmax[0] = pars->ferm_mass * pars->ferm_mass;

@@ -141,24 +141,30 @@ int ostaple_invert_mixed_batch(const su3_soa* u, const double_soa* phases, doubl
   return ok ? INVERTER_SUCCESS : INVERTER_FAILURE;
 }
 
-int ostaple_multishift_batch(const su3_soa* u, const double_soa* phases, double mass, const RationalApprox* approx,
-                             int nrhs, const vec3_soa* sources, vec3_soa* solutions, double res, int max_iter,
-                             double delta_frac, int* iters_cgm, int* iters_refine, double* true_res) {
-  if (!require_init("ostaple_multishift_batch")) return INVERTER_FAILURE;
-  const int order = approx->approx_order;
+}  // extern "C"
+
+namespace ost {
+
+// All shifts of one rational approximation for nrhs <= 4 right-hand sides
+// in two phases.  Phase A: one FP32 CG-M for all right-hand sides together
+// (each link read once per Dslash for all of them) to the relative residual
+// res_cgm.  Phase B (refine != 0): every (rhs, shift) system refined from the
+// FP32 result to an FP64 true residual <= res by the batched mixed solver,
+// in batches that group the same shift of all right-hand sides.  Without
+// phase B the FP32 solutions are returned as FP64.  xs64[r*order + k] is the
+// solution of (M^+M + shifts[k]) x = b_r.
+int multishift_two_phase(const double2* u64, const double* ph64, double mass, const double* shifts, int order,
+                         int nrhs, const double2* b64, double2* xs64, double res_cgm, double res, int max_iter,
+                         double delta_frac, int refine, int* iters_cgm, int* iters_refine, double* true_res) {
+  typedef double2 Z;
   if (nrhs < 1 || nrhs > 4 || order < 1 || order > CGM_MAX_SHIFTS) {
-    set_error(-11, "ostaple_multishift_batch: nrhs %d (1..4), order %d (1..%d)", nrhs, order, CGM_MAX_SHIFTS);
+    set_error(-11, "multi-shift solve: nrhs %d (1..4), order %d (1..%d)", nrhs, order, CGM_MAX_SHIFTS);
     return INVERTER_FAILURE;
   }
   cudaStream_t st = rt().stream;
   const long n = 3L * rt().g.sizeh;
-  const Z* u64 = dev(reinterpret_cast<const Z*>(u), "u");
-  const void* ph = resolve(phases, "phases");
-  Z* xs64 = dev(reinterpret_cast<Z*>(solutions), "solutions");
-  const Z* b64 = dev(reinterpret_cast<const Z*>(sources), "sources");
-  if (!u64 || !ph || !xs64 || !b64) return INVERTER_FAILURE;
   Prepared pr;
-  if (!prepare(u64, static_cast<const double*>(ph), &pr, st)) return INVERTER_FAILURE;
+  if (!prepare(u64, ph64, &pr, st)) return INVERTER_FAILURE;
   // phase A: FP32 CG-M for all right-hand sides together
   const size_t nv = size_t(nrhs) * (2 * order + 5);
   float2* f = static_cast<float2*>(workspace(WS_MULTI, nv * n * sizeof(float2)));
@@ -174,20 +180,17 @@ int ostaple_multishift_batch(const su3_soa* u, const double_soa* phases, double 
   C.s = C.p + nrhs * n;
   C.t = C.s + nrhs * n;
   conv_d2f(b64, bf, nrhs * n, st);
-  // phase A (FP32 CG-M) runs to 100 x the target: every extra decade of its
-  // recursive residual saves refinement iterations in phase B.  Measured at
-  // 32^4, m = 0.01, 4 sources x 19 shifts: 1e-5 -> 620 ms, 1e-6 -> 557 ms,
-  // 1e-7 -> 504 ms, 1e-8 -> 496 ms, 1e-9 -> 506 ms.
-  const double res_a = 100.0 * res;
-  CgmBatchResult ra = batched_cgm_f32(C, mass * mass, approx->RA_b, res_a, max_iter, st);
+  CgmBatchResult ra = batched_cgm_f32(C, mass * mass, shifts, res_cgm, max_iter, st);
   for (int r = 0; r < nrhs; ++r)
     if (iters_cgm) iters_cgm[r] = ra.iters[r];
-  // phase B: every (rhs, shift) system refined from the FP32 result to an
-  // FP64 true residual <= res, in batches that group the same shift of all
-  // right-hand sides
   const long total = long(nrhs) * order;
   k_f2d_copy<<<8 * rt().num_sms, 256, 0, st>>>(C.xs, xs64, total * n);
   OST_LAUNCH_CHECK();
+  if (!refine) {
+    OST_CUDA(cudaStreamSynchronize(st));
+    return error_code() ? INVERTER_FAILURE : INVERTER_SUCCESS;
+  }
+  // phase B
   BatchScal* sc = batch_scalars();
   if (!sc) return INVERTER_FAILURE;
   DfOperator dop{};
@@ -210,11 +213,11 @@ int ostaple_multishift_batch(const su3_soa* u, const double_soa* phases, double 
       const int r = sys_rhs[s0 + k], sh = sys_shift[s0 + k];
       OST_CUDA(cudaMemcpyAsync(sx + k * n, xs64 + (long(r) * order + sh) * n, n * sizeof(Z), cudaMemcpyDeviceToDevice, st));
       OST_CUDA(cudaMemcpyAsync(sb + k * n, b64 + r * n, n * sizeof(Z), cudaMemcpyDeviceToDevice, st));
-      m2[k] = mass * mass + approx->RA_b[sh];
+      m2[k] = mass * mass + shifts[sh];
     }
     BatchBuffers B{};
     if (!batch_buffers(m, &B)) return INVERTER_FAILURE;
-    B.u64 = u64; B.ph64 = ph; B.u32 = pr.u32; B.ph32 = pr.ph; B.ph32_mode = pr.mode;
+    B.u64 = u64; B.ph64 = ph64; B.u32 = pr.u32; B.ph32 = pr.ph; B.ph32_mode = pr.mode;
     B.q16 = pr.q16; B.uq = pr.uq;
     B.use_df = use_df;
     B.df = dop;
@@ -233,6 +236,28 @@ int ostaple_multishift_batch(const su3_soa* u, const double_soa* phases, double 
   OST_CUDA(cudaStreamSynchronize(st));
   if (error_code()) return INVERTER_FAILURE;
   return ok ? INVERTER_SUCCESS : INVERTER_FAILURE;
+}
+
+}  // namespace ost
+
+extern "C" {
+
+int ostaple_multishift_batch(const su3_soa* u, const double_soa* phases, double mass, const RationalApprox* approx,
+                             int nrhs, const vec3_soa* sources, vec3_soa* solutions, double res, int max_iter,
+                             double delta_frac, int* iters_cgm, int* iters_refine, double* true_res) {
+  if (!require_init("ostaple_multishift_batch")) return INVERTER_FAILURE;
+  const Z* u64 = dev(reinterpret_cast<const Z*>(u), "u");
+  const void* ph = resolve(phases, "phases");
+  Z* xs64 = dev(reinterpret_cast<Z*>(solutions), "solutions");
+  const Z* b64 = dev(reinterpret_cast<const Z*>(sources), "sources");
+  if (!u64 || !ph || !xs64 || !b64) return INVERTER_FAILURE;
+  // phase A (FP32 CG-M) runs to 100 x the target: every extra decade of its
+  // recursive residual saves refinement iterations in phase B.  Measured at
+  // 32^4, m = 0.01, 4 sources x 19 shifts: 1e-5 -> 620 ms, 1e-6 -> 557 ms,
+  // 1e-7 -> 504 ms, 1e-8 -> 496 ms, 1e-9 -> 506 ms.
+  return multishift_two_phase(u64, static_cast<const double*>(ph), mass, approx->RA_b, approx->approx_order, nrhs,
+                              b64, xs64, 100.0 * res, res, max_iter, delta_frac, 1, iters_cgm, iters_refine,
+                              true_res);
 }
 
 }  // extern "C"

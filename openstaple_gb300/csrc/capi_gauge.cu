@@ -2,8 +2,11 @@
 // force (stouting.h:13-44, fermion_force.h:15-36,
 // fermion_force_utilities.h:204-240), plus the multi-shift dispatch wrapper
 // (inverter_wrappers.c:41-114).
+#include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
+#include "batched.cuh"
 #include "dslash.cuh"
 #include "gauge_kernels.cuh"
 #include "kernels.cuh"
@@ -35,6 +38,76 @@ template <typename T> T* D(T* p, const char* n) { return static_cast<T*>(resolve
 template <typename T> const T* D(const T* p, const char* n) { return static_cast<const T*>(resolve(p, n)); }
 
 void zero_bytes(void* p, size_t n) { OST_CUDA(cudaMemsetAsync(p, 0, n, S())); }
+
+
+// The pseudofermions of one flavour in groups of up to 4: all shifts of a
+// group solved together by the two-phase multi-shift solver (FP32 CG-M to the
+// reference's single-precision target, then FP64 refinement: batched mixed
+// when mixed != 0, else ker_invert_openacc per system), then D_oe of every
+// solution and the outer products of the whole group accumulated into aux in
+// one pass (fermion_force.c:222-249 loops over the pseudofermions one by one).
+// The last pseudofermion's solutions are left in shiftmulti and its last
+// shift's X and D_oe X in ip.loc_s / ip.loc_h, as after the reference's loop.
+void force_pseudofermion_groups(inverter_package ip, ferm_param* fp, const Z* first_src, su3_soa* aux_u,
+                                vec3_soa* shiftmulti, double res, int max_cg, int mixed) {
+  const int order = fp->approx_md.approx_order;
+  const int nps = fp->number_of_ps;
+  if (order < 1 || order > MAX_APPROX_ORDER) {
+    set_error(-11, "fermion force: approx_md order %d out of range", order);
+    return;
+  }
+  const long n = vlen();
+  const Z* u = D(reinterpret_cast<const Z*>(ip.u), "ip.u");
+  const double* ph = static_cast<const double*>(resolve(fp->phases, "phases"));
+  const Z* b = D(first_src, "ferm_in_acc");
+  Z* aux = D(reinterpret_cast<Z*>(aux_u), "aux_u");
+  Z* last = D(reinterpret_cast<Z*>(shiftmulti), "tferm_shiftmulti_acc");
+  const int group = std::min(nps, 4);
+  Z* xs = static_cast<Z*>(workspace(WS_FORCE1, size_t(group) * order * n * sizeof(Z)));
+  Z* ys = static_cast<Z*>(workspace(WS_MULTI2, std::max<size_t>(size_t(group) * order * n * sizeof(Z),
+                                                                2 * size_t(BATCH_MAX) * n * sizeof(Z))));
+  double* coef = static_cast<double*>(workspace(WS_FORCE3, 128 * sizeof(double)));
+  if (!u || !ph || !b || !aux || !last || !xs || !ys || !coef) return;
+  double res_sp = double(8e-7f * sqrtf(float(sh())));
+  if (res_sp < res) res_sp = res;
+  double c[128];
+  for (int p0 = 0; p0 < nps; p0 += 4) {
+    const int m = std::min(4, nps - p0);
+    int it_cgm[4];
+    int st = multishift_two_phase(u, ph, fp->ferm_mass, fp->approx_md.RA_b, order, m, b + long(p0) * n, xs, res_sp,
+                                  res, max_cg, 0.0, mixed, it_cgm, nullptr, nullptr);
+    convergence_messages(CONVERGENCE_NONCRITICAL, st);
+    if (!mixed) {
+      for (int r = 0; r < m; ++r)
+        for (int k = 0; k < order; ++k) {
+          vec3_soa* xk = reinterpret_cast<vec3_soa*>(xs + (long(r) * order + k) * n);
+          const vec3_soa* src = reinterpret_cast<const vec3_soa*>(b + long(p0 + r) * n);
+          inverter_wrapper(ip, fp, xk, src, res, max_cg, fp->approx_md.RA_b[k], CONVERGENCE_NONCRITICAL);
+        }
+    }
+    // ys = D_oe xs (the ys buffer is reused by the refinement stage, so after it)
+    for (int k = 0; k < m * order; ++k) {
+      DslashArgs<double> a;
+      a.parity = 1; a.phase_mode = PH_ANGLE; a.epilogue = EPI_PLAIN; a.u = u; a.out = ys + k * n;
+      a.in = xs + k * n; a.phases = ph; a.in0 = nullptr; a.mass2 = 0; a.stream = S(); a.compact_links = 0;
+      launch_dslash<double>(a);
+    }
+    for (int r = 0; r < m; ++r)
+      for (int k = 0; k < order; ++k) c[r * order + k] = fp->approx_md.RA_a[k];
+    OST_CUDA(cudaMemcpyAsync(coef, c, size_t(m) * order * sizeof(double), cudaMemcpyHostToDevice, S()));
+    launch_force_outer(xs, ys, n, m * order, coef, nullptr, aux, 0, S());
+    if (p0 + m == nps) {
+      const Z* xl = xs + long(m - 1) * order * n;
+      blas_copy<double>(xl, last, long(order) * n, S());
+      Z* s = ip.loc_s ? D(reinterpret_cast<Z*>(ip.loc_s), "loc_s") : nullptr;
+      Z* h = ip.loc_h ? D(reinterpret_cast<Z*>(ip.loc_h), "loc_h") : nullptr;
+      if (s) blas_copy<double>(xl + (order - 1) * n, s, n, S());
+      if (h) blas_copy<double>(ys + (long(m - 1) * order + order - 1) * n, h, n, S());
+    }
+    // the host coefficient buffer is reused by the next group
+    OST_CUDA(cudaStreamSynchronize(S()));
+  }
+}
 
 }  // namespace
 
@@ -131,7 +204,7 @@ void direct_product_of_fermions_into_auxmat(const vec3_soa* loc_s, const vec3_so
   const Z* x = D(reinterpret_cast<const Z*>(loc_s), "loc_s");
   const Z* y = D(reinterpret_cast<const Z*>(loc_h), "loc_h");
   Z* aux = D(reinterpret_cast<Z*>(aux_u), "aux_u");
-  double* coef = static_cast<double*>(workspace(WS_FORCE3, 64 * sizeof(double)));
+  double* coef = static_cast<double*>(workspace(WS_FORCE3, 128 * sizeof(double)));
   if (!x || !y || !aux || !coef) return;
   OST_CUDA(cudaMemcpyAsync(coef, &approx->RA_a[iter], sizeof(double), cudaMemcpyHostToDevice, S()));
   launch_force_outer(x, y, vlen(), 1, coef, nullptr, aux, 0, S());
@@ -146,7 +219,7 @@ void ker_openacc_compute_fermion_force(const su3_soa* u, su3_soa* aux_u, const v
   const Z* xs = D(reinterpret_cast<const Z*>(in_shiftmulti), "in_shiftmulti");
   const void* ph = resolve(tpars->phases, "phases");
   Z* ys = static_cast<Z*>(workspace(WS_MULTI2, size_t(order > 0 ? order : 1) * vlen() * sizeof(Z)));
-  double* coef = static_cast<double*>(workspace(WS_FORCE3, 64 * sizeof(double)));
+  double* coef = static_cast<double*>(workspace(WS_FORCE3, 128 * sizeof(double)));
   if (!du || !aux || !xs || !ph || !ys || !coef || order < 1 || order > MAX_APPROX_ORDER) {
     if (order < 1 || order > MAX_APPROX_ORDER) set_error(-11, "approx_md order %d out of range", order);
     return;
@@ -183,23 +256,57 @@ void multiply_conf_times_force_and_take_ta_nophase(const su3_soa* u, const su3_s
   if (du && aux && ip) launch_conf_force_ta(du, aux, ip, S());
 }
 
-// Multi-shift solve dispatch (inverter_wrappers.c:41-114).  The
-// single-precision-accelerated branch of the reference (SP multi-shift then
-// a DP refinement per shift) maps to a mixed-precision refinement of each
-// shift here, started from the FP64 multi-shift result.
+// Multi-shift solve dispatch (inverter_wrappers.c:41-114).
+//
+// Default: the FP64 multishift_invert to res.  With
+// inverter_tricks.singlePInvAccelMultiInv, as in the reference, a
+// single-precision CG-M runs first to max(8e-7 sqrt(sizeh), res) (:57-60) and
+// every shift is then refined to res in FP64: with useMixedPrecision all
+// shifts together by the batched mixed solver (each to an FP64 true residual
+// <= res), otherwise one after the other by ker_invert_openacc from the
+// single-precision guess (inverter_wrapper, :82-96).  The single-precision
+// phase is the library's FP32 CG-M on its own FP32 copy of ip.u (ip.u_f is
+// not read).  Returns the total iteration count: the CG-M iterations plus
+// those of every refinement (the reference adds the CG-M count once per
+// shift instead, :97; no caller reads it).
 int inverter_multishift_wrapper(inverter_package ip, ferm_param* pars, RationalApprox* approx, vec3_soa* out,
                                 const vec3_soa* in, double res, int max_cg, int convergence_importance) {
-  int cg = 0, total = 0;
-  int st = multishift_invert(ip.u, pars, approx, out, in, res, ip.loc_r, ip.loc_h, ip.loc_s, ip.loc_p,
-                             ip.ferm_shift_temp, max_cg, &cg);
+  int cg = 0;
+  if (!inverter_tricks.singlePInvAccelMultiInv) {
+    const int st = multishift_invert(ip.u, pars, approx, out, in, res, ip.loc_r, ip.loc_h, ip.loc_s, ip.loc_p,
+                                     ip.ferm_shift_temp, max_cg, &cg);
+    convergence_messages(convergence_importance, st);
+    return cg;
+  }
+  if (!require_init("inverter_multishift_wrapper")) return 0;
+  const int order = approx->approx_order;
+  const Z* u = D(reinterpret_cast<const Z*>(ip.u), "ip.u");
+  const double* ph = static_cast<const double*>(resolve(pars->phases, "phases"));
+  const Z* b = D(reinterpret_cast<const Z*>(in), "in");
+  Z* xs = D(reinterpret_cast<Z*>(out), "out");
+  if (!u || !ph || !b || !xs) {
+    convergence_messages(convergence_importance, INVERTER_FAILURE);
+    return 0;
+  }
+  double res_sp = double(8e-7f * sqrtf(float(sh())));
+  if (res_sp < res) res_sp = res;
+  int it_cgm = 0, total = 0;
+  if (inverter_tricks.useMixedPrecision) {
+    int it_ref[MAX_APPROX_ORDER] = {0};
+    const int st = multishift_two_phase(u, ph, pars->ferm_mass, approx->RA_b, order, 1, b, xs, res_sp, res, max_cg,
+                                        0.0, 1, &it_cgm, it_ref, nullptr);
+    total = it_cgm;
+    for (int k = 0; k < order; ++k) total += it_ref[k];
+    convergence_messages(convergence_importance, st);
+    return total;
+  }
+  const int st = multishift_two_phase(u, ph, pars->ferm_mass, approx->RA_b, order, 1, b, xs, res_sp, res, max_cg,
+                                      0.0, 0, &it_cgm, nullptr, nullptr);
   convergence_messages(convergence_importance, st);
-  total += cg;
-  if (inverter_tricks.singlePInvAccelMultiInv) {
-    const long n = vlen();
-    for (int k = 0; k < approx->approx_order; ++k) {
-      vec3_soa* xk = reinterpret_cast<vec3_soa*>(reinterpret_cast<Z*>(out) + k * n);
-      total += inverter_wrapper(ip, pars, xk, in, res, max_cg, approx->RA_b[k], convergence_importance);
-    }
+  total = it_cgm;
+  for (int k = 0; k < order; ++k) {
+    vec3_soa* xk = reinterpret_cast<vec3_soa*>(reinterpret_cast<Z*>(out) + k * vlen());
+    total += inverter_wrapper(ip, pars, xk, in, res, max_cg, approx->RA_b[k], convergence_importance);
   }
   return total;
 }
@@ -224,12 +331,23 @@ void fermion_force_soloopenacc(su3_soa* tconf_acc, su3_soa* tstout_conf_acc_arr,
   for (int f = 0; f < tNDiffFlavs; ++f) {
     ferm_param* fp = &tfermion_parameters[f];
     set_su3_soa_to_zero(taux_conf_acc);
-    for (int ps = 0; ps < fp->number_of_ps; ++ps) {
-      const vec3_soa* src = reinterpret_cast<const vec3_soa*>(reinterpret_cast<const Z*>(ferm_in_acc) +
-                                                              long(fp->index_of_the_first_ps + ps) * vlen());
-      inverter_multishift_wrapper(ipt, fp, &fp->approx_md, tferm_shiftmulti_acc, src, res, max_cg,
-                                  CONVERGENCE_NONCRITICAL);
-      ker_openacc_compute_fermion_force(ipt.u, taux_conf_acc, tferm_shiftmulti_acc, ipt.loc_s, ipt.loc_h, fp);
+    const Z* first_src = reinterpret_cast<const Z*>(ferm_in_acc) + long(fp->index_of_the_first_ps) * vlen();
+    if (inverter_tricks.singlePInvAccelMultiInv && fp->number_of_ps > 1 && !inverter_tricks.useMixedPrecision) {
+      // accelerated mode with FP64 refinement: the pseudofermions share one
+      // FP32 CG-M launch sequence per group of 4, each shift then refined
+      // by ker_invert_openacc, and all outer products of a group in one pass
+      force_pseudofermion_groups(ipt, fp, first_src, taux_conf_acc, tferm_shiftmulti_acc, res, max_cg, 0);
+    } else if (inverter_tricks.singlePInvAccelMultiInv && fp->number_of_ps > 1) {
+      // accelerated mode with mixed refinement: FP32 CG-M and refinement of
+      // every (pseudofermion, shift) system batched
+      force_pseudofermion_groups(ipt, fp, first_src, taux_conf_acc, tferm_shiftmulti_acc, res, max_cg, 1);
+    } else {
+      for (int ps = 0; ps < fp->number_of_ps; ++ps) {
+        const vec3_soa* src = reinterpret_cast<const vec3_soa*>(first_src + long(ps) * vlen());
+        inverter_multishift_wrapper(ipt, fp, &fp->approx_md, tferm_shiftmulti_acc, src, res, max_cg,
+                                    CONVERGENCE_NONCRITICAL);
+        ker_openacc_compute_fermion_force(ipt.u, taux_conf_acc, tferm_shiftmulti_acc, ipt.loc_s, ipt.loc_h, fp);
+      }
     }
     multiply_backfield_times_force(fp, taux_conf_acc, gl3_aux);
   }

@@ -61,6 +61,55 @@ void fused_cgm_update(typename cplx_t<T>::type* p, const typename cplx_t<T>::typ
   OST_LAUNCH_CHECK();
 }
 
+// x_k -= om_k * ps_k for every active shift k, all shifts in one pass
+// (multiple_combine_in1_minus_in2x_factor_back_into_in1,
+// fermionic_utilities.c:315-339)
+template <typename C, typename S>
+__global__ void k_multi_xupdate(C* x, const C* __restrict__ ps, long stride, CgmCoeffs cf, long n) {
+  OST_GRID_LOOP(i, n) {
+    for (int k = 0; k < cf.nshift; ++k) {
+      if (!cf.active[k]) continue;
+      C xv = x[k * stride + i], pv = ps[k * stride + i];
+      const S om = S(cf.omega[k]);
+      x[k * stride + i] = cmk<C>(fma(-om, pv.x, xv.x), fma(-om, pv.y, xv.y));
+    }
+  }
+}
+
+// ps_k = ga_k * ps_k + ze_k * r for every active shift k
+// (multiple1_combine_in1_x_fact1_plus_in2_x_fact2_back_into_in1,
+// fermionic_utilities.c:341-377)
+template <typename C, typename S>
+__global__ void k_multi_pupdate(C* ps, const C* __restrict__ r, long stride, CgmCoeffs cf, long n) {
+  OST_GRID_LOOP(i, n) {
+    const C rr = r[i];
+    for (int k = 0; k < cf.nshift; ++k) {
+      if (!cf.active[k]) continue;
+      C pv = ps[k * stride + i];
+      const S ga = S(cf.gamma[k]), ze = S(cf.zeta[k]);
+      ps[k * stride + i] = cmk<C>(fma(ga, pv.x, ze * rr.x), fma(ga, pv.y, ze * rr.y));
+    }
+  }
+}
+
+template <typename T>
+void multi_xupdate(typename cplx_t<T>::type* x, const typename cplx_t<T>::type* ps, long stride, const CgmCoeffs& cf,
+                   long n, cudaStream_t st) {
+  long b = (n + 255) / 256;
+  long cap = 8L * rt().num_sms;
+  k_multi_xupdate<typename cplx_t<T>::type, T><<<int(b < cap ? b : cap), 256, 0, st>>>(x, ps, stride, cf, n);
+  OST_LAUNCH_CHECK();
+}
+
+template <typename T>
+void multi_pupdate(typename cplx_t<T>::type* ps, const typename cplx_t<T>::type* r, long stride, const CgmCoeffs& cf,
+                   long n, cudaStream_t st) {
+  long b = (n + 255) / 256;
+  long cap = 8L * rt().num_sms;
+  k_multi_pupdate<typename cplx_t<T>::type, T><<<int(b < cap ? b : cap), 256, 0, st>>>(ps, r, stride, cf, n);
+  OST_LAUNCH_CHECK();
+}
+
 // out = a0*in + sum_k a_k x_k
 template <typename C>
 __global__ void k_recombine(const C* __restrict__ xs, long stride, const C* __restrict__ in, C* out, RecombCoeffs rc,
@@ -93,6 +142,10 @@ template void fused_cgm_update<double>(double2*, const double2*, double, double2
                                        const CgmCoeffs&, long, cudaStream_t);
 template void fused_cgm_update<float>(float2*, const float2*, double, float2*, float2*, long, const CgmCoeffs&,
                                       long, cudaStream_t);
+template void multi_xupdate<double>(double2*, const double2*, long, const CgmCoeffs&, long, cudaStream_t);
+template void multi_xupdate<float>(float2*, const float2*, long, const CgmCoeffs&, long, cudaStream_t);
+template void multi_pupdate<double>(double2*, const double2*, long, const CgmCoeffs&, long, cudaStream_t);
+template void multi_pupdate<float>(float2*, const float2*, long, const CgmCoeffs&, long, cudaStream_t);
 template void recombine<double>(const double2*, long, const double2*, double2*, const RecombCoeffs&, long,
                                 cudaStream_t);
 template void recombine<float>(const float2*, long, const float2*, float2*, const RecombCoeffs&, long,

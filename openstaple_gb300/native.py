@@ -181,6 +181,32 @@ SIGNATURES = {
                                          InverterPackage, _I]),
     "inverter_multishift_wrapper": (_I, [InverterPackage, C.POINTER(FermParam), C.POINTER(RationalApprox), _P, _P,
                                          _D, _I, _I]),
+    # single-precision twins (sp_*.c) and float <-> double conversions
+    "acc_Deo_f": (None, [_P, _P, _P, _P]),
+    "acc_Doe_f": (None, [_P, _P, _P, _P]),
+    "acc_Deo_unsafe_f": (None, [_P, _P, _P, _P]),
+    "acc_Doe_unsafe_f": (None, [_P, _P, _P, _P]),
+    "fermion_matrix_multiplication_f": (None, [_P, _P, _P, _P, C.POINTER(FermParam)]),
+    "fermion_matrix_multiplication_shifted_f": (None, [_P, _P, _P, _P, C.POINTER(FermParam), C.c_float]),
+    "l2norm2_global_f": (_D, [_P]),
+    "real_scal_prod_global_f": (_D, [_P, _P]),
+    "set_vec3_soa_to_zero_f": (None, [_P]),
+    "assign_in_to_out_f": (None, [_P, _P]),
+    "combine_in1xfactor_plus_in2_f": (None, [_P, _D, _P, _P]),
+    "combine_add_factor_x_in2_to_in1_f": (None, [_P, _P, _D]),
+    "combine_in1xferm_mass_minus_in2_f": (None, [_P, _D, _P]),
+    "combine_in1_minus_in2_f": (None, [_P, _P, _P]),
+    "multiply_fermion_x_doublefactor_f": (None, [_P, _D]),
+    "ker_invert_openacc_f": (_I, [_P, C.POINTER(FermParam), _P, _P, _D, _P, _P, _P, _P, _I, _D, C.POINTER(_I)]),
+    "multishift_invert_f": (_I, [_P, C.POINTER(FermParam), C.POINTER(RationalApprox), _P, _P, _D, _P, _P, _P, _P,
+                                 _P, _I, C.POINTER(_I)]),
+    "recombine_shifted_vec3_to_vec3_f": (None, [_P, _P, _P, C.POINTER(RationalApprox)]),
+    "convert_double_to_float_vec3_soa": (None, [_P, _P]),
+    "convert_float_to_double_vec3_soa": (None, [_P, _P]),
+    "convert_double_to_float_real_soa": (None, [_P, _P]),
+    "convert_float_to_double_real_soa": (None, [_P, _P]),
+    "convert_double_to_float_su3_soa": (None, [_P, _P]),
+    "convert_float_to_double_su3_soa": (None, [_P, _P]),
 }
 
 _lib = None
