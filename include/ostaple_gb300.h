@@ -44,6 +44,7 @@ typedef struct thmat_soa_t thmat_soa;     /* c01,c02,c12 complex; rc00,rc11  */
 typedef struct vec3_soa_f_t vec3_soa_f;   /* float twins (generated sp_ types) */
 typedef struct su3_soa_f_t su3_soa_f;
 typedef struct float_soa_t float_soa;
+typedef struct dcomplex_soa_t dcomplex_soa; /* c[sizeh] double complex     */
 
 #define INVERTER_SUCCESS 1                /* inverter_full.h:12 */
 #define INVERTER_FAILURE 0                /* inverter_full.h:13 */
@@ -128,6 +129,27 @@ typedef struct action_param_t {           /* OpenAcc/action.h:8-20 */
   double topo_rho;
 } action_param;
 #endif
+
+#ifndef OSTAPLE_HAVE_REFERENCE_TYPES
+typedef struct md_param_t {               /* OpenAcc/md_parameters.h:7-20 */
+  int no_md;
+  int gauge_scale;
+  double t;
+  double residue_metro;
+  double expected_max_eigenvalue;
+  int singlePrecMD;
+  double residue_md;
+  int max_cg_iterations;
+  int recycleInvsForce;
+  int extrapolateInvsForce;
+} md_param;
+#endif
+
+/* Molecular-dynamics parameters and the integrator step sizes
+ * (md_parameters.c:8-9, 57).  Weak library defaults; a host definition
+ * overrides them. */
+extern md_param md_parameters;
+extern double deltas_Omelyan[7];
 
 /* Stout parameters read by stout_wrapper / fermion_force_soloopenacc and the
  * stout kernels (action.h:22-23).  Weak library defaults: 2 steps of
@@ -431,6 +453,64 @@ void fermion_force_soloopenacc(su3_soa *tconf_acc, su3_soa *tstout_conf_acc_arr,
  * shift is then refined by inverter_wrapper (inverter_wrappers.c:41-114) */
 int inverter_multishift_wrapper(inverter_package ip, ferm_param *pars, RationalApprox *approx, vec3_soa *out,
                                 const vec3_soa *in, double res, int max_cg, int convergence_importance);
+
+/* ---- pure-gauge tree-level Symanzik HMC (ipdot_gauge.h, plaquettes.h,
+ * rectangles.h, su3_utilities.h, su3_measurements.h, md_integrator.h,
+ * md_parameters.h, random_assignement.h) ------------------------------------
+ * Staples are dS/dU summed over the paths that close link (x, mu):
+ * C_ZERO = 5/3 times the plaquette staples, C_ONE = -1/12 times the 2x1
+ * rectangle staples of types A, B, C; each function ADDS its part. */
+void calc_loc_staples_nnptrick_all(const su3_soa *u, su3_soa *loc_stap);                  /* plaquettes.h:16 */
+void calc_loc_improved_staples_typeA_nnptrick_all(const su3_soa *u, su3_soa *loc_stap);   /* rectangles.h:40 */
+void calc_loc_improved_staples_typeB_nnptrick_all(const su3_soa *u, su3_soa *loc_stap);   /* rectangles.h:42 */
+void calc_loc_improved_staples_typeC_nnptrick_all(const su3_soa *u, su3_soa *loc_stap);   /* rectangles.h:44 */
+/* tipdot = TA(U loc_stap) (su3_utilities.h:41) */
+void conf_times_staples_ta_part(const su3_soa *u, const su3_soa *loc_stap, tamat_soa *tipdot);
+/* the whole gauge force: local_staples = dS/dU (if not NULL), tipdot = TA(U dS/dU)
+ * (ipdot_gauge.h, ipdot_gauge.c:361-426) */
+void calc_ipdot_gauge_soloopenacc(const su3_soa *tconf_acc, su3_soa *local_staples, tamat_soa *tipdot);
+/* sum over sites and planes mu < nu of Re tr of the plaquettes / of the 2x1
+ * and 1x2 rectangles (su3_measurements.h:14, rectangles.h:80); the parking
+ * arguments are not used */
+double calc_plaquette_soloopenacc(su3_soa *tconf_acc, su3_soa *local_plaqs, dcomplex_soa *tr_local_plaqs);
+double calc_rettangolo_soloopenacc(const su3_soa *tconf_acc, su3_soa *local_plaqs, dcomplex_soa *tr_local_plaqs);
+/* sum over the links of direction mu (0..7) of 1/2 tr P^2 (su3_measurements.h:11) */
+double calc_momenta_action(const thmat_soa *mom, double_soa *tr_local, const int mu);
+/* mom -= i factor[id] ipdot (complex entries), += on the real diagonals (su3_utilities.h:53) */
+void mom_sum_mult(thmat_soa *mom, const tamat_soa *ipdot, const double *factor, int id_factor);
+/* U = exp(i tdelta[id] P) U, rows 0-1 reunitarised (su3_utilities.h:58) */
+void mom_exp_times_conf_soloopenacc(su3_soa *tconf_acc, const thmat_soa *tmomenta, const double *tdelta,
+                                    int id_delta);
+/* deltas_Omelyan from md_params and act_params.beta (md_parameters.h:25) */
+void initialize_md_global_variables(md_param md_params);
+/* one gauge multistep of the 2MN integrator with md_parameters.gauge_scale
+ * substeps and the steps in deltas_Omelyan (md_integrator.h:14) */
+void multistep_2MN_gauge(su3_soa *tconf_acc, su3_soa *local_staples, tamat_soa *tipdot, thmat_soa *tmomenta);
+/* Gaussian momenta into the HOST array mom8 (8 thmat_soa), as the
+ * reference's (random_assignement.h:26); the deviates come from the
+ * library's counter-based generator seeded by ostaple_set_momenta_seed (no
+ * reference counterpart), not from the reference's dSFMT stream */
+void generate_Momenta_gauss(thmat_soa *mom8);
+void ostaple_set_momenta_seed(unsigned long long seed);
+
+/* Link generator (no reference counterpart): ntraj pure-gauge tree-level
+ * Symanzik HMC trajectories of length traj_len with the reference's
+ * integrator (no_md steps, each two gauge multisteps of gauge_scale 2MN
+ * substeps: md_integrator.c:347-376, 502-742 without fermions), Metropolis
+ * on exp(-delta S) when metropolis != 0.  Momenta come from the counter-based
+ * generator (seed, trajectory first_traj + k).  precision 0: FP64 molecular
+ * dynamics; 1: FP32 molecular dynamics (force, kicks and link updates) from
+ * the FP64 links, the result reunitarised in FP64, actions and Metropolis in
+ * FP64.  plaquette[k] (<Re tr P>/3 after trajectory k) and delta_s[k] may be
+ * NULL.  Returns 0 or an error code. */
+int ostaple_pure_gauge_hmc(su3_soa *u, double beta, int ntraj, int no_md, int gauge_scale, double traj_len,
+                           unsigned long long seed, int first_traj, int precision, int metropolis, int *accepted,
+                           double *plaquette, double *delta_s);
+/* Gaussian momenta on the device from (seed, stream); the same counter-based
+ * generator the host field helpers use */
+int ostaple_gauge_momenta(thmat_soa *mom, unsigned long long seed, unsigned long long stream);
+/* plaquette and rectangle sums and the action -beta/3 (C_ZERO P + C_ONE R) */
+int ostaple_gauge_action(const su3_soa *u, double beta, double *plaq_sum, double *rect_sum, double *action);
 
 /* Mixed-precision CG that iterates until the FP64 true residual
  * sqrt(|b - (M^+M + shift) x|^2 / |b|^2) is <= res (or max_iter), with a

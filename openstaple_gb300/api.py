@@ -280,6 +280,82 @@ def multiply_conf_times_force_and_take_ta_nophase(u, auxmat, ipdot) -> None:
     check(0, "multiply_conf_times_force_and_take_ta_nophase")
 
 
+# ---- pure-gauge tree-level Symanzik HMC ----
+def calc_ipdot_gauge_soloopenacc(u, local_staples, tipdot) -> None:
+    lib().calc_ipdot_gauge_soloopenacc(ptr(u), None if local_staples is None else ptr(local_staples), ptr(tipdot))
+    check(0, "calc_ipdot_gauge_soloopenacc")
+
+
+def calc_plaquette_soloopenacc(u) -> float:
+    v = lib().calc_plaquette_soloopenacc(ptr(u), None, None)
+    check(0, "calc_plaquette_soloopenacc")
+    return v
+
+
+def calc_rettangolo_soloopenacc(u) -> float:
+    v = lib().calc_rettangolo_soloopenacc(ptr(u), None, None)
+    check(0, "calc_rettangolo_soloopenacc")
+    return v
+
+
+def momenta_action(mom) -> float:
+    """sum over the 8 directions of calc_momenta_action (1/2 tr P^2 over all links)."""
+    v = sum(lib().calc_momenta_action(ptr(mom), None, mu) for mu in range(8))
+    check(0, "calc_momenta_action")
+    return v
+
+
+def mom_sum_mult(mom, ipdot, factor: float) -> None:
+    f = (C.c_double * 1)(factor)
+    lib().mom_sum_mult(ptr(mom), ptr(ipdot), f, 0)
+    check(0, "mom_sum_mult")
+
+
+def mom_exp_times_conf_soloopenacc(u, mom, delta: float) -> None:
+    f = (C.c_double * 1)(delta)
+    lib().mom_exp_times_conf_soloopenacc(ptr(u), ptr(mom), f, 0)
+    check(0, "mom_exp_times_conf_soloopenacc")
+
+
+def multistep_2MN_gauge(u, local_staples, tipdot, mom, beta: float, no_md: int, gauge_scale: int, t: float,
+                        ncalls: int = 1) -> None:
+    """ncalls x multistep_2MN_gauge with deltas_Omelyan set by
+    initialize_md_global_variables for (beta, no_md, gauge_scale, t)."""
+    from .native import MdParam, act_params, md_parameters
+    act_params().beta = float(beta)
+    mp = md_parameters()
+    mp.no_md, mp.gauge_scale, mp.t = int(no_md), int(gauge_scale), float(t)
+    lib().initialize_md_global_variables(mp)
+    for _ in range(ncalls):
+        lib().multistep_2MN_gauge(ptr(u), ptr(local_staples), ptr(tipdot), ptr(mom))
+    check(0, "multistep_2MN_gauge")
+
+
+def pure_gauge_hmc(u, beta: float, ntraj: int, no_md: int = 18, gauge_scale: int = 4, traj_len: float = 1.0,
+                   seed: int = 1, first_traj: int = 0, precision: str = "fp64", metropolis: bool = True) -> dict:
+    """ntraj pure-gauge tree-level Symanzik HMC trajectories on the links u
+    (updated in place on the device); precision "fp64" or "fp32" (FP32
+    molecular dynamics, FP64 actions and Metropolis)."""
+    acc = C.c_int(0)
+    plaq = np.zeros(max(ntraj, 1))
+    ds = np.zeros(max(ntraj, 1))
+    rc = lib().ostaple_pure_gauge_hmc(ptr(u), beta, ntraj, no_md, gauge_scale, traj_len, seed, first_traj,
+                                      {"fp64": 0, "fp32": 1}[precision], int(metropolis), C.byref(acc),
+                                      plaq.ctypes.data, ds.ctypes.data)
+    check(rc, "ostaple_pure_gauge_hmc")
+    return dict(accepted=acc.value, plaquette=plaq[:ntraj], delta_s=ds[:ntraj])
+
+
+def gauge_momenta(mom, seed: int, stream: int) -> None:
+    check(lib().ostaple_gauge_momenta(ptr(mom), seed, stream), "ostaple_gauge_momenta")
+
+
+def gauge_action(u, beta: float) -> dict:
+    p, r, s = C.c_double(0), C.c_double(0), C.c_double(0)
+    check(lib().ostaple_gauge_action(ptr(u), beta, C.byref(p), C.byref(r), C.byref(s)), "ostaple_gauge_action")
+    return dict(plaq_sum=p.value, rect_sum=r.value, action=s.value)
+
+
 # ---- batched solvers ----
 def invert_mixed_batch(u, phases, mass: float, solutions, sources, shifts=None, res: float = 1e-10,
                        max_iter: int = 100000, delta_frac: float = 0.0) -> dict:

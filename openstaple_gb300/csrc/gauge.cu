@@ -15,9 +15,7 @@ static constexpr double C_ZERO = 5.0 * 0.33333333333333333333333;   // tree-leve
 
 // Small-c1 table: exp(iQ) = sum_n (iQ)^n/n! with Q^n reduced by Q^3 = c1 Q + c0
 // to polynomials in (c0, c1), truncated at total weight 7 (c0: 3, c1: 2).
-void ensure_ch_table(cudaStream_t st) {
-  static bool done = false;
-  if (done) return;
+void fill_ch_table(CHTable* table) {
   const int mons[8][2] = {{0, 0}, {0, 1}, {0, 2}, {0, 3}, {1, 0}, {1, 1}, {1, 2}, {2, 0}};
   auto index = [&](int i, int j) {
     for (int k = 0; k < 8; ++k)
@@ -48,10 +46,16 @@ void ensure_ch_table(cudaStream_t st) {
     inr = -ini / double(n + 1);
     ini = t / double(n + 1);
   }
-  CHTable h;
   for (int j = 0; j < 3; ++j)
-    for (int k = 0; k < 8; ++k) h.f[j][k] = make_double2(fr[j][k], fi[j][k]);
-  for (int k = 0; k < 8; ++k) { h.i0[k] = mons[k][0]; h.j1[k] = mons[k][1]; }
+    for (int k = 0; k < 8; ++k) table->f[j][k] = make_double2(fr[j][k], fi[j][k]);
+  for (int k = 0; k < 8; ++k) { table->i0[k] = mons[k][0]; table->j1[k] = mons[k][1]; }
+}
+
+void ensure_ch_table(cudaStream_t st) {
+  static bool done = false;
+  if (done) return;
+  CHTable h;
+  fill_ch_table(&h);
   OST_CUDA(cudaMemcpyToSymbolAsync(c_ch_table, &h, sizeof(h), 0, cudaMemcpyHostToDevice, st));
   OST_CUDA(cudaStreamSynchronize(st));
   done = true;

@@ -198,8 +198,11 @@ OST_D TA ta_of(const M3& m, double s) {
 // Small c1 (< 4e-3): polynomial in (c0, c1) truncated at total weight 7
 // (weight 3 for c0, 2 for c1), table built on the host (gauge.cu).
 struct CHTable { double2 f[3][8]; int i0[8]; int j1[8]; };
-// Filled once by ensure_ch_table(); this header is included by gauge.cu only.
+// Every translation unit that includes this header has its own copy of the
+// table in constant memory and uploads fill_ch_table()'s values before use
+// (gauge.cu: ensure_ch_table, hmc.cu: its own).
 static __constant__ CHTable c_ch_table;
+void fill_ch_table(CHTable* table);   // host, gauge.cu
 
 struct CHCoeffs { double2 f[3], b1[3], b2[3]; };
 

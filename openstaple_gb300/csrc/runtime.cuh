@@ -105,6 +105,9 @@ enum WorkspaceSlot {
   WS_LINKS_LO,     // lo parts of the double-float links
   WS_DF,           // double-float M^+M work fields
   WS_LINKS_Q16,    // 16-bit fixed-point sloppy links
+  WS_HMC_MOM,      // link generator: FP64 momenta
+  WS_HMC_BKP,      // link generator: links before the trajectory (Metropolis reject)
+  WS_HMC_F32,      // link generator: FP32 links and momenta of the molecular dynamics
   WS_NSLOTS
 };
 

@@ -129,3 +129,32 @@ def site_parity_index(dims):
     lex = (x + n0 * (y + n1 * (z + n2 * t))).ravel()
     par = ((x + y + z + t) % 2).ravel()
     return lex, par, lex // 2
+
+
+def cold_links(dims) -> np.ndarray:
+    """Every link the identity (a cold start), complex128 (8, 3, 3, sizeh)."""
+    sh = sizeh(dims)
+    u = np.zeros((8, 3, 3, sh), np.complex128)
+    for r in range(3):
+        u[:, r, r] = 1.0
+    return u
+
+
+def gauge_momenta(dims, seed: int, stream: int) -> np.ndarray:
+    """The traceless Hermitian momenta thmat_soa[8], float64 (8, 8*sizeh),
+    that the library's device generator makes from (seed, stream): per link
+    eight normal deviates g of variance 1/2 (the counter-based generator of
+    this module) composed as random_assignement.c:173-177:
+    rc00 = g2 + g7/sqrt(3), rc11 = -g2 + g7/sqrt(3), c01 = g0 - i g1,
+    c02 = g3 - i g4, c12 = g5 - i g6."""
+    sh = sizeh(dims)
+    g = gaussians(seed, 64 * sh, stream).reshape(8, sh, 8)
+    r3 = 1.0 / np.sqrt(3.0)
+    mom = np.zeros((8, 8 * sh))
+    c = mom[:, :6 * sh].view(np.complex128).reshape(8, 3, sh)
+    c[:, 0] = g[:, :, 0] - 1j * g[:, :, 1]
+    c[:, 1] = g[:, :, 3] - 1j * g[:, :, 4]
+    c[:, 2] = g[:, :, 5] - 1j * g[:, :, 6]
+    mom[:, 6 * sh:7 * sh] = g[:, :, 2] + g[:, :, 7] * r3
+    mom[:, 7 * sh:] = -g[:, :, 2] + g[:, :, 7] * r3
+    return mom

@@ -181,6 +181,24 @@ SIGNATURES = {
                                          InverterPackage, _I]),
     "inverter_multishift_wrapper": (_I, [InverterPackage, C.POINTER(FermParam), C.POINTER(RationalApprox), _P, _P,
                                          _D, _I, _I]),
+    # pure-gauge tree-level Symanzik HMC
+    "calc_loc_staples_nnptrick_all": (None, [_P, _P]),
+    "calc_loc_improved_staples_typeA_nnptrick_all": (None, [_P, _P]),
+    "calc_loc_improved_staples_typeB_nnptrick_all": (None, [_P, _P]),
+    "calc_loc_improved_staples_typeC_nnptrick_all": (None, [_P, _P]),
+    "conf_times_staples_ta_part": (None, [_P, _P, _P]),
+    "calc_ipdot_gauge_soloopenacc": (None, [_P, _P, _P]),
+    "calc_plaquette_soloopenacc": (_D, [_P, _P, _P]),
+    "calc_rettangolo_soloopenacc": (_D, [_P, _P, _P]),
+    "calc_momenta_action": (_D, [_P, _P, _I]),
+    "mom_sum_mult": (None, [_P, _P, C.POINTER(_D), _I]),
+    "mom_exp_times_conf_soloopenacc": (None, [_P, _P, C.POINTER(_D), _I]),
+    "multistep_2MN_gauge": (None, [_P, _P, _P, _P]),
+    "generate_Momenta_gauss": (None, [_P]),
+    "ostaple_set_momenta_seed": (None, [C.c_ulonglong]),
+    "ostaple_pure_gauge_hmc": (_I, [_P, _D, _I, _I, _I, _D, C.c_ulonglong, _I, _I, _I, C.POINTER(_I), _P, _P]),
+    "ostaple_gauge_momenta": (_I, [_P, C.c_ulonglong, C.c_ulonglong]),
+    "ostaple_gauge_action": (_I, [_P, _D, C.POINTER(_D), C.POINTER(_D), C.POINTER(_D)]),
     # single-precision twins (sp_*.c) and float <-> double conversions
     "acc_Deo_f": (None, [_P, _P, _P, _P]),
     "acc_Doe_f": (None, [_P, _P, _P, _P]),
@@ -224,8 +242,29 @@ def lib() -> C.CDLL:
             f = getattr(L, name)
             f.restype = res
             f.argtypes = args
+        L.initialize_md_global_variables.restype = None
+        L.initialize_md_global_variables.argtypes = [MdParam]
         _lib = L
     return _lib
+
+
+class MdParam(C.Structure):
+    """Layout of the reference's md_param (OpenAcc/md_parameters.h:7-20)."""
+    _fields_ = [
+        ("no_md", C.c_int), ("gauge_scale", C.c_int), ("t", C.c_double), ("residue_metro", C.c_double),
+        ("expected_max_eigenvalue", C.c_double), ("singlePrecMD", C.c_int), ("residue_md", C.c_double),
+        ("max_cg_iterations", C.c_int), ("recycleInvsForce", C.c_int), ("extrapolateInvsForce", C.c_int),
+    ]
+
+
+def md_parameters() -> "MdParam":
+    """The library's `md_parameters` global (writable)."""
+    return MdParam.in_dll(lib(), "md_parameters")
+
+
+def deltas_omelyan():
+    """The library's `deltas_Omelyan[7]` global."""
+    return (C.c_double * 7).in_dll(lib(), "deltas_Omelyan")
 
 
 class ActionParam(C.Structure):

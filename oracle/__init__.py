@@ -55,6 +55,15 @@ class Oracle:
         "orc_force_outer": (None, [_P, _P, _P, _P, _I, _P]),
         "orc_backfield_times_force": (None, [_P, _P, _P]),
         "orc_conf_times_force_ta": (None, [_P, _P, _P]),
+        "orc_gauge_staples": (None, [_P, _P]),
+        "orc_ipdot_gauge": (None, [_P, _P]),
+        "orc_plaquette_sum": (_D, [_P]),
+        "orc_rectangle_sum": (_D, [_P]),
+        "orc_momenta_action": (_D, [_P]),
+        "orc_mom_sum_mult": (None, [_P, _P, _D]),
+        "orc_mom_exp_times_conf": (None, [_P, _P, _D]),
+        "orc_md_deltas": (None, [_D, _I, _I, _D, _P]),
+        "orc_2mn_gauge": (None, [_P, _P, _D, _I, _I, _D, _I]),
     }
 
     def __init__(self, dims, threads: int = 1):
@@ -189,6 +198,47 @@ class Oracle:
         self.L.orc_conf_times_force_ta(_p(u), _p(sigma), _p(out))
         return out
 
+    # --- pure-gauge tree-level Symanzik HMC ---
+    def gauge_staples(self, u):
+        s = self.su3()
+        self.L.orc_gauge_staples(_p(u), _p(s))
+        return s
+
+    def plaquette_sum(self, u):
+        return self.L.orc_plaquette_sum(_p(u))
+
+    def rectangle_sum(self, u):
+        return self.L.orc_rectangle_sum(_p(u))
+
+    def momenta_action(self, mom):
+        return self.L.orc_momenta_action(_p(np.ascontiguousarray(mom)))
+
+    def mom_sum_mult(self, mom, ipdot, fact):
+        out = np.ascontiguousarray(mom).copy()
+        self.L.orc_mom_sum_mult(_p(out), _p(np.ascontiguousarray(ipdot)), fact)
+        return out
+
+    def mom_exp_times_conf(self, u, mom, delta):
+        out = u.copy()
+        self.L.orc_mom_exp_times_conf(_p(out), _p(np.ascontiguousarray(mom)), delta)
+        return out
+
+    def md_deltas(self, beta, no_md, gauge_scale, t):
+        d = np.zeros(7)
+        self.L.orc_md_deltas(beta, no_md, gauge_scale, t, _p(d))
+        return d
+
+    def gauge_2mn(self, u, mom, beta, no_md, gauge_scale, t, ncalls):
+        """(U, P) after ncalls x multistep_2MN_gauge; a pure-gauge trajectory is 2 no_md calls."""
+        uo, mo = u.copy(), np.ascontiguousarray(mom).copy()
+        self.L.orc_2mn_gauge(_p(uo), _p(mo), beta, no_md, gauge_scale, t, ncalls)
+        return uo, mo
+
+    def ipdot_gauge(self, u):
+        ip = self.tamat()
+        self.L.orc_ipdot_gauge(_p(u), _p(ip))
+        return ip
+
 
 def ref_available(dims) -> bool:
     return (REF_DIR / ("libref_" + "x".join(map(str, dims)) + ".so")).exists()
@@ -233,6 +283,15 @@ class Reference:
         "ref_sigma": (None, [_P, _P, _P, _P, _D]),
         "ref_stout_wrapper": (None, [_P, _P, _I, _D]),
         "ref_fermion_force": (None, [_P, _P, _P, _P, _D, _I, _I, _P, _P, _P, _D, _I, _I, _D]),
+        "ref_gauge_staples": (None, [_P, _P]),
+        "ref_ipdot_gauge": (None, [_P, _P, _P]),
+        "ref_plaquette_sum": (_D, [_P]),
+        "ref_rectangle_sum": (_D, [_P]),
+        "ref_momenta_action": (_D, [_P]),
+        "ref_mom_sum_mult": (None, [_P, _P, _D]),
+        "ref_mom_exp_times_conf": (None, [_P, _P, _D]),
+        "ref_md_deltas": (None, [_D, _I, _I, _D, _P]),
+        "ref_2mn_gauge": (None, [_P, _P, _D, _I, _I, _D, _I]),
     }
 
     def __init__(self, dims):
@@ -379,4 +438,46 @@ class Reference:
         ph = np.ascontiguousarray(ph)
         self.L.ref_fermion_force(_p(u), _p(lv), _p(ip), _p(ph), mass, len(phis), len(a), _p(a), _p(b), _p(phis),
                                  res, max_cg, steps, rho)
+        return ip
+
+    # --- pure-gauge tree-level Symanzik HMC ---
+    def gauge_staples(self, u):
+        s = self.su3()
+        self.L.ref_gauge_staples(_p(u), _p(s))
+        return s
+
+    def plaquette_sum(self, u):
+        return self.L.ref_plaquette_sum(_p(u))
+
+    def rectangle_sum(self, u):
+        return self.L.ref_rectangle_sum(_p(u))
+
+    def momenta_action(self, mom):
+        return self.L.ref_momenta_action(_p(np.ascontiguousarray(mom)))
+
+    def mom_sum_mult(self, mom, ipdot, fact):
+        out = np.ascontiguousarray(mom).copy()
+        self.L.ref_mom_sum_mult(_p(out), _p(np.ascontiguousarray(ipdot)), fact)
+        return out
+
+    def mom_exp_times_conf(self, u, mom, delta):
+        out = u.copy()
+        self.L.ref_mom_exp_times_conf(_p(out), _p(np.ascontiguousarray(mom)), delta)
+        return out
+
+    def md_deltas(self, beta, no_md, gauge_scale, t):
+        d = np.zeros(7)
+        self.L.ref_md_deltas(beta, no_md, gauge_scale, t, _p(d))
+        return d
+
+    def gauge_2mn(self, u, mom, beta, no_md, gauge_scale, t, ncalls):
+        """(U, P) after ncalls x multistep_2MN_gauge; a pure-gauge trajectory is 2 no_md calls."""
+        uo, mo = u.copy(), np.ascontiguousarray(mom).copy()
+        self.L.ref_2mn_gauge(_p(uo), _p(mo), beta, no_md, gauge_scale, t, ncalls)
+        return uo, mo
+
+    def ipdot_gauge(self, u):
+        ip = self.tamat()
+        st = self.su3()
+        self.L.ref_ipdot_gauge(_p(u), _p(st), _p(ip))
         return ip

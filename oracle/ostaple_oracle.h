@@ -55,4 +55,15 @@ void orc_force_outer(const ocplx *u, ocplx *aux, const ocplx *xs, const double *
 void orc_backfield_times_force(const double *ph, const ocplx *aux, ocplx *pip);
 void orc_conf_times_force_ta(const ocplx *u, const ocplx *sigma, double *ipdot);
 
+/* pure-gauge tree-level Symanzik HMC (ostaple_oracle_gauge.c) */
+void orc_gauge_staples(const ocplx *u, ocplx *stap);
+void orc_ipdot_gauge(const ocplx *u, double *ipdot);
+double orc_plaquette_sum(const ocplx *u);
+double orc_rectangle_sum(const ocplx *u);
+double orc_momenta_action(double *mom);
+void orc_mom_sum_mult(double *mom, double *ipdot, double fact);
+void orc_mom_exp_times_conf(ocplx *u, double *mom, double delta);
+void orc_md_deltas(double beta, int no_md, int gauge_scale, double t, double *d);
+void orc_2mn_gauge(ocplx *u, double *mom, double beta, int no_md, int gauge_scale, double t, int ncalls);
+
 #endif

@@ -495,3 +495,225 @@ void orc_ch_coeffs(double c0, double c1, double *out)
     out[12 + 2 * j] = creal(b2[j]); out[13 + 2 * j] = cimag(b2[j]);
   }
 }
+
+/* ==== pure-gauge tree-level Symanzik HMC (restated from ipdot_gauge.c,
+ * plaquettes.c, rectangles.c, su3_utilities.c, su3_measurements.c,
+ * md_integrator.c, md_parameters.c) ==== */
+
+#define C_ONE (-0.25 * 0.33333333333333333333333)   /* tree-level Symanzik c1 (common_defines.h:75) */
+
+/* link U_mu(x + a e_s + b e_t), its parity taken from the shifted site */
+static M3 lk(const ocplx *u, const int d[4], int mu, int s, int a, int t, int b)
+{
+  int e[4] = {d[0], d[1], d[2], d[3]};
+  e[s] = ((e[s] + a) % NN[s] + NN[s]) % NN[s];
+  e[t] = ((e[t] + b) % NN[t] + NN[t]) % NN[t];
+  int p = (e[0] + e[1] + e[2] + e[3]) & 1;
+  return ld_link(u, 2 * mu + p, sn(e));
+}
+
+static M3 m5(M3 a, M3 b, M3 c, M3 d, M3 e) { return mmul(mmul(mmul(mmul(a, b), c), d), e); }
+
+/* dS/dU of the tree-level Symanzik action for the link (x, mu), the
+ * closing paths from x+mu back to x: C_ZERO x the 6 plaquette staples
+ * (plaquettes.c:83-195) + C_ONE x the 18 rectangle staples of types A, B, C
+ * (rectangles.c:643-917):
+ *   A_R = U_n(x+m) U_n(x+m+n) U_m(x+2n)^+ U_n(x+n)^+ U_n(x)^+
+ *   A_L = U_n(x+m-n)^+ U_n(x+m-2n)^+ U_m(x-2n)^+ U_n(x-2n) U_n(x-n)
+ *   B_R = U_m(x+m) U_n(x+2m) U_m(x+m+n)^+ U_m(x+n)^+ U_n(x)^+
+ *   B_L = U_m(x+m) U_n(x+2m-n)^+ U_m(x+m-n)^+ U_m(x-n)^+ U_n(x-n)
+ *   C_R = U_n(x+m) U_m(x+n)^+ U_m(x-m+n)^+ U_n(x-m)^+ U_m(x-m)
+ *   C_L = U_n(x+m-n)^+ U_m(x-n)^+ U_m(x-m-n)^+ U_n(x-m-n) U_m(x-m) */
+static M3 gauge_staple(const ocplx *u, const int d[4], int m)
+{
+  M3 pl = mzero(), re = mzero();
+  for (int n = 0; n < 4; n++) {
+    if (n == m) continue;
+    M3 r = mmul(mmul(lk(u, d, n, m, 1, n, 0), mdag(lk(u, d, m, n, 1, m, 0))), mdag(lk(u, d, n, m, 0, n, 0)));
+    M3 l = mmul(mmul(mdag(lk(u, d, n, m, 1, n, -1)), mdag(lk(u, d, m, n, -1, m, 0))), lk(u, d, n, n, -1, m, 0));
+    pl = madd(pl, madd(r, l));
+    M3 ar = m5(lk(u, d, n, m, 1, n, 0), lk(u, d, n, m, 1, n, 1), mdag(lk(u, d, m, n, 2, m, 0)),
+               mdag(lk(u, d, n, n, 1, m, 0)), mdag(lk(u, d, n, n, 0, m, 0)));
+    M3 al = m5(mdag(lk(u, d, n, m, 1, n, -1)), mdag(lk(u, d, n, m, 1, n, -2)), mdag(lk(u, d, m, n, -2, m, 0)),
+               lk(u, d, n, n, -2, m, 0), lk(u, d, n, n, -1, m, 0));
+    M3 br = m5(lk(u, d, m, m, 1, n, 0), lk(u, d, n, m, 2, n, 0), mdag(lk(u, d, m, m, 1, n, 1)),
+               mdag(lk(u, d, m, n, 1, m, 0)), mdag(lk(u, d, n, n, 0, m, 0)));
+    M3 bl = m5(lk(u, d, m, m, 1, n, 0), mdag(lk(u, d, n, m, 2, n, -1)), mdag(lk(u, d, m, m, 1, n, -1)),
+               mdag(lk(u, d, m, n, -1, m, 0)), lk(u, d, n, n, -1, m, 0));
+    M3 cr = m5(lk(u, d, n, m, 1, n, 0), mdag(lk(u, d, m, n, 1, m, 0)), mdag(lk(u, d, m, m, -1, n, 1)),
+               mdag(lk(u, d, n, m, -1, n, 0)), lk(u, d, m, m, -1, n, 0));
+    M3 cl = m5(mdag(lk(u, d, n, m, 1, n, -1)), mdag(lk(u, d, m, n, -1, m, 0)), mdag(lk(u, d, m, m, -1, n, -1)),
+               lk(u, d, n, m, -1, n, -1), lk(u, d, m, m, -1, n, 0));
+    re = madd(re, madd(madd(madd(ar, al), madd(br, bl)), madd(cr, cl)));
+  }
+  return madd(mscale(pl, C_ZERO), mscale(re, C_ONE));
+}
+
+void orc_gauge_staples(const ocplx *u, ocplx *stap)
+{
+  int d[4];
+  for (d[3] = 0; d[3] < NN[3]; d[3]++)
+    for (d[2] = 0; d[2] < NN[2]; d[2]++)
+      for (d[1] = 0; d[1] < NN[1]; d[1]++)
+        for (d[0] = 0; d[0] < NN[0]; d[0]++) {
+          int p = (d[0] + d[1] + d[2] + d[3]) & 1;
+          for (int mu = 0; mu < 4; mu++) st_full(stap, 2 * mu + p, sn(d), gauge_staple(u, d, mu), 3);
+        }
+}
+
+/* tipdot = TA(U dS/dU) for every link (ipdot_gauge.c:192-212 +
+ * su3_utilities.c:146-175, su3_utilities.h:979-1035) */
+void orc_ipdot_gauge(const ocplx *u, double *ipdot)
+{
+  int d[4];
+  for (d[3] = 0; d[3] < NN[3]; d[3]++)
+    for (d[2] = 0; d[2] < NN[2]; d[2]++)
+      for (d[1] = 0; d[1] < NN[1]; d[1]++)
+        for (d[0] = 0; d[0] < NN[0]; d[0]++) {
+          int p = (d[0] + d[1] + d[2] + d[3]) & 1;
+          long x = sn(d);
+          for (int mu = 0; mu < 4; mu++) {
+            int dir = 2 * mu + p;
+            st_ta(ipdot, dir, x, mmul(ld_link(u, dir, x), gauge_staple(u, d, mu)), 1.0);
+          }
+        }
+}
+
+/* sum over sites and planes mu < nu of Re tr of the plaquette
+ * U_mu(x) U_nu(x+mu) U_mu(x+nu)^+ U_nu(x)^+ (su3_measurements.c:191-213,
+ * plaquettes.c:14-80) */
+double orc_plaquette_sum(const ocplx *u)
+{
+  double s = 0;
+  int d[4];
+  for (d[3] = 0; d[3] < NN[3]; d[3]++)
+    for (d[2] = 0; d[2] < NN[2]; d[2]++)
+      for (d[1] = 0; d[1] < NN[1]; d[1]++)
+        for (d[0] = 0; d[0] < NN[0]; d[0]++)
+          for (int m = 0; m < 3; m++)
+            for (int n = m + 1; n < 4; n++) {
+              M3 pq = mmul(mmul(lk(u, d, m, m, 0, n, 0), lk(u, d, n, m, 1, n, 0)),
+                           mmul(mdag(lk(u, d, m, n, 1, m, 0)), mdag(lk(u, d, n, m, 0, n, 0))));
+              s += creal(mtr(pq));
+            }
+  return s;
+}
+
+/* sum over sites and planes mu < nu of Re tr of the 2x1 and 1x2 rectangles
+ * (rectangles.c:16-164, 1890-1909):
+ *   U_m(x) U_m(x+m) U_n(x+2m) U_m(x+m+n)^+ U_m(x+n)^+ U_n(x)^+
+ *   U_m(x) U_n(x+m) U_n(x+m+n) U_m(x+2n)^+ U_n(x+n)^+ U_n(x)^+ */
+double orc_rectangle_sum(const ocplx *u)
+{
+  double s = 0;
+  int d[4];
+  for (d[3] = 0; d[3] < NN[3]; d[3]++)
+    for (d[2] = 0; d[2] < NN[2]; d[2]++)
+      for (d[1] = 0; d[1] < NN[1]; d[1]++)
+        for (d[0] = 0; d[0] < NN[0]; d[0]++)
+          for (int m = 0; m < 3; m++)
+            for (int n = m + 1; n < 4; n++) {
+              M3 a = mmul(m5(lk(u, d, m, m, 0, n, 0), lk(u, d, m, m, 1, n, 0), lk(u, d, n, m, 2, n, 0),
+                             mdag(lk(u, d, m, m, 1, n, 1)), mdag(lk(u, d, m, n, 1, m, 0))),
+                          mdag(lk(u, d, n, m, 0, n, 0)));
+              M3 b = mmul(m5(lk(u, d, m, m, 0, n, 0), lk(u, d, n, m, 1, n, 0), lk(u, d, n, m, 1, n, 1),
+                             mdag(lk(u, d, m, n, 2, m, 0)), mdag(lk(u, d, n, n, 1, m, 0))),
+                          mdag(lk(u, d, n, m, 0, n, 0)));
+              s += creal(mtr(a)) + creal(mtr(b));
+            }
+  return s;
+}
+
+/* sum over all links of 1/2 tr P^2 = a^2 + b^2 + ab + |c01|^2 + |c02|^2 + |c12|^2
+ * (su3_measurements.c:138-168, su3_utilities.h:1295-1307) */
+double orc_momenta_action(double *mom)
+{
+  double s = 0;
+  for (int dir = 0; dir < 8; dir++)
+    for (long i = 0; i < SHH; i++) {
+      double a = blk_r(mom, dir, 0)[i], b = blk_r(mom, dir, 1)[i];
+      ocplx c = blk_c(mom, dir, 0)[i], e = blk_c(mom, dir, 1)[i], f = blk_c(mom, dir, 2)[i];
+      s += a * a + b * b + a * b + creal(c) * creal(c) + cimag(c) * cimag(c) + creal(e) * creal(e) +
+           cimag(e) * cimag(e) + creal(f) * creal(f) + cimag(f) * cimag(f);
+    }
+  return s;
+}
+
+/* mom -= i fact ipdot on the complex entries, mom_kk += fact ipdot_kk on the
+ * real diagonals (su3_utilities.c:241-270, su3_utilities.h:1383-1395) */
+void orc_mom_sum_mult(double *mom, double *ipdot, double fact)
+{
+  for (int dir = 0; dir < 8; dir++)
+    for (long i = 0; i < SHH; i++) {
+      for (int k = 0; k < 3; k++) blk_c(mom, dir, k)[i] -= I * fact * blk_c(ipdot, dir, k)[i];
+      for (int k = 0; k < 2; k++) blk_r(mom, dir, k)[i] += fact * blk_r(ipdot, dir, k)[i];
+    }
+}
+
+/* U = exp(i delta P) U with rows 0-1 reunitarised by Gram-Schmidt
+ * (su3_utilities.c:272-305, su3_utilities.h:1433-1537): exp(-Q_A) of the
+ * anti-Hermitian Q_A = -i delta P */
+void orc_mom_exp_times_conf(ocplx *u, double *mom, double delta)
+{
+  double *qa = calloc(64 * SHH, sizeof(double));
+  for (int dir = 0; dir < 8; dir++)
+    for (long i = 0; i < SHH; i++) {
+      for (int k = 0; k < 3; k++) blk_c(qa, dir, k)[i] = -blk_c(mom, dir, k)[i] * delta * I;
+      for (int k = 0; k < 2; k++) blk_r(qa, dir, k)[i] = -blk_r(mom, dir, k)[i] * delta;
+    }
+  for (int dir = 0; dir < 8; dir++)
+    for (long i = 0; i < SHH; i++) {
+      double c0, c1;
+      M3 q = q_of(qa, dir, i, &c0, &c1);
+      ocplx f[3], b1[3], b2[3];
+      ch_coeffs(c0, c1, f, b1, b2, 0);
+      M3 r = mmul(poly(f[0], f[1], f[2], q, mmul(q, q)), ld_link(u, dir, i));
+      double n0 = 0;
+      for (int c = 0; c < 3; c++) n0 += creal(r.m[0][c]) * creal(r.m[0][c]) + cimag(r.m[0][c]) * cimag(r.m[0][c]);
+      n0 = 1.0 / sqrt(n0);
+      for (int c = 0; c < 3; c++) r.m[0][c] *= n0;
+      ocplx sp = conj(r.m[0][0]) * r.m[1][0] + conj(r.m[0][1]) * r.m[1][1] + conj(r.m[0][2]) * r.m[1][2];
+      for (int c = 0; c < 3; c++) r.m[1][c] -= sp * r.m[0][c];
+      double n1 = 0;
+      for (int c = 0; c < 3; c++) n1 += creal(r.m[1][c]) * creal(r.m[1][c]) + cimag(r.m[1][c]) * cimag(r.m[1][c]);
+      n1 = 1.0 / sqrt(n1);
+      for (int c = 0; c < 3; c++) r.m[1][c] *= n1;
+      st_full(u, dir, i, r, 2);
+    }
+  free(qa);
+}
+
+/* the integrator coefficients of initialize_md_global_variables
+ * (md_parameters.c:11-50; Omelyan lambda = 0.1931833275037836) */
+void orc_md_deltas(double beta, int no_md, int gauge_scale, double t, double *d)
+{
+  const double lambda = 0.1931833275037836;
+  const double b3 = beta * 0.33333333333333333333333;
+  d[0] = -t / no_md * lambda;
+  d[1] = -t / no_md * (1.0 - 2.0 * lambda);
+  d[2] = -t / no_md * 2.0 * lambda;
+  d[3] = -t / (2 * no_md * gauge_scale) * lambda * b3;
+  d[4] = 0.5 * t / (2 * no_md * gauge_scale);
+  d[5] = -t / (2 * no_md * gauge_scale) * (1.0 - 2.0 * lambda) * b3;
+  d[6] = -t / (2 * no_md * gauge_scale) * 2.0 * lambda * b3;
+}
+
+/* ncalls x multistep_2MN_gauge (md_integrator.c:256-376):
+ *   K(d3) X [K(d5) X K(d6) X]^(gauge_scale-1) K(d5) X K(d3)
+ * with K(f): mom += f TA(U dS/dU) and X: U = exp(i d4 P) U */
+void orc_2mn_gauge(ocplx *u, double *mom, double beta, int no_md, int gauge_scale, double t, int ncalls)
+{
+  double d[7];
+  orc_md_deltas(beta, no_md, gauge_scale, t, d);
+  double *ip = calloc(64 * SHH, sizeof(double));
+  for (int c = 0; c < ncalls; c++) {
+    orc_ipdot_gauge(u, ip); orc_mom_sum_mult(mom, ip, d[3]); orc_mom_exp_times_conf(u, mom, d[4]);
+    for (int k = 1; k < gauge_scale; k++) {
+      orc_ipdot_gauge(u, ip); orc_mom_sum_mult(mom, ip, d[5]); orc_mom_exp_times_conf(u, mom, d[4]);
+      orc_ipdot_gauge(u, ip); orc_mom_sum_mult(mom, ip, d[6]); orc_mom_exp_times_conf(u, mom, d[4]);
+    }
+    orc_ipdot_gauge(u, ip); orc_mom_sum_mult(mom, ip, d[5]); orc_mom_exp_times_conf(u, mom, d[4]);
+    orc_ipdot_gauge(u, ip); orc_mom_sum_mult(mom, ip, d[3]);
+  }
+  free(ip);
+}

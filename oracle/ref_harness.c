@@ -46,6 +46,11 @@
 #include "../Include/fermion_parameters.h"
 #include "../DbgTools/dbgtools.h"
 #include "./su3_measurements.h"
+#include "./ipdot_gauge.h"
+#include "./rectangles.h"
+#include "./md_parameters.h"
+#include "./md_integrator.h"
+#include "./alloc_settings.h"
 #include "./sp_struct_c_def.h"
 #include "./sp_alloc_vars.h"
 
@@ -63,12 +68,23 @@ debug_settings_t debug_settings;
 md_param md_parameters;
 int md_dbg_print_count, md_diag_count_fermion, ipdot_f_reset, nMdInversionPerformed;
 
-/* stubs for diagnostics that the wrapped paths never reach at verbosity 0 */
-void check_unitarity_device(const su3_soa *u, double *mx, double *avg) { *mx = 0; *avg = 0; }
-double calc_force_norm(const tamat_soa *t) { return 0.0; }
-double calc_diff_force_norm(const tamat_soa *a, const tamat_soa *b) { return 0.0; }
-void copy_ipdot_into_old(const tamat_soa *a, tamat_soa *b) {}
+tamat_soa *ipdot_g_old;
+int ipdot_g_reset, md_diag_count_gauge;
+/* the benchmark drivers' timing container (test_and_benchmarks.h:31-44) */
+typedef struct { double t[16]; int count; } harness_md_times;
+harness_md_times gauge_mdtimes;
+
+/* stubs for diagnostics and for parts the wrapped paths never reach at
+ * verbosity 0 (the topological force is off: act_params.topo_action = 0) */
 void dbg_print_su3_soa(su3_soa *const conf, const char *n, int i) {}
+void dbgprint_gl3_soa(su3_soa *const conf, const char *n, int i) {}
+void print_tamat_soa(tamat_soa *const t, const char *n) {}
+void print_thmat_soa(thmat_soa *const t, const char *n) {}
+void print_gl3_soa_wrapper(const su3_soa *t, const char *n) {}
+void print_tamat_soa_wrapper(const tamat_soa *t, const char *n) {}
+void print_thmat_soa_wrapper(const thmat_soa *t, const char *n) {}
+void calc_ipdot_topo(const su3_soa *const u, su3_soa *const s, su3_soa *a, su3_soa *const b,
+                     tamat_soa *const ip) {}
 void convert_double_to_float_su3_soa(const su3_soa *d, su3_soa_f *f) {}
 
 /* The double-precision branch of the reference's inverter_multishift_wrapper
@@ -372,4 +388,92 @@ void ref_fermion_force(const double *u, double *levels, double *ipdot, double *p
   free(aux_th); free(aux_ta);
   aux_th = NULL; aux_ta = NULL;
   stout_globals(0);
+}
+
+/* ---- pure-gauge tree-level Symanzik HMC pieces (ipdot_gauge.c,
+ * plaquettes.c, rectangles.c, su3_utilities.c, su3_measurements.c,
+ * md_integrator.c, md_parameters.c) ---- */
+
+/* the gauge staples dS/dU: C_ZERO x plaquette staples + C_ONE x the three
+ * rectangle types (ipdot_gauge.c:192-212) */
+void ref_gauge_staples(const double *u, double *stap)
+{
+  set_su3_soa_to_zero((su3_soa *)stap);
+  calc_loc_staples_nnptrick_all((const su3_soa *)u, (su3_soa *)stap);
+  calc_loc_improved_staples_typeA_nnptrick_all((const su3_soa *)u, (su3_soa *)stap);
+  calc_loc_improved_staples_typeB_nnptrick_all((const su3_soa *)u, (su3_soa *)stap);
+  calc_loc_improved_staples_typeC_nnptrick_all((const su3_soa *)u, (su3_soa *)stap);
+}
+
+/* tipdot = TA(U staples) (ipdot_gauge.c:361-426) */
+void ref_ipdot_gauge(const double *u, double *stap, double *ipdot)
+{
+  calc_ipdot_gauge_soloopenacc((const su3_soa *)u, (su3_soa *)stap, (tamat_soa *)ipdot);
+}
+
+double ref_plaquette_sum(const double *u)
+{
+  su3_soa *lp = xalloc(2 * sizeof(su3_soa));
+  dcomplex_soa *tr = xalloc(2 * sizeof(dcomplex_soa));
+  double r = calc_plaquette_soloopenacc((su3_soa *)u, lp, tr);
+  free(lp); free(tr);
+  return r;
+}
+
+double ref_rectangle_sum(const double *u)
+{
+  su3_soa *lp = xalloc(2 * sizeof(su3_soa));
+  dcomplex_soa *tr = xalloc(2 * sizeof(dcomplex_soa));
+  double r = calc_rettangolo_soloopenacc((const su3_soa *)u, lp, tr);
+  free(lp); free(tr);
+  return r;
+}
+
+/* sum over the 8 link directions of 1/2 tr P^2 (su3_measurements.c:138-168) */
+double ref_momenta_action(const double *mom)
+{
+  double_soa *tr = xalloc(sizeof(double_soa));
+  double r = 0;
+  for (int mu = 0; mu < 8; mu++) r += calc_momenta_action((const thmat_soa *)mom, tr, mu);
+  free(tr);
+  return r;
+}
+
+/* mom += factor x ipdot (su3_utilities.c:241-270) */
+void ref_mom_sum_mult(double *mom, const double *ipdot, double factor)
+{
+  double f[1] = {factor};
+  mom_sum_mult((thmat_soa *)mom, (const tamat_soa *)ipdot, f, 0);
+}
+
+/* U = exp(i delta P) U, rows 0-1 reunitarised (su3_utilities.c:272-305) */
+void ref_mom_exp_times_conf(double *u, const double *mom, double delta)
+{
+  double f[1] = {delta};
+  mom_exp_times_conf_soloopenacc((su3_soa *)u, (const thmat_soa *)mom, f, 0);
+}
+
+/* the integrator steps of initialize_md_global_variables (md_parameters.c:11-50) */
+void ref_md_deltas(double beta, int no_md, int gauge_scale, double t, double *d7)
+{
+  act_params.beta = beta;
+  md_parameters.no_md = no_md;
+  md_parameters.gauge_scale = gauge_scale;
+  md_parameters.t = t;
+  initialize_md_global_variables(md_parameters);
+  for (int i = 0; i < 7; i++) d7[i] = deltas_Omelyan[i];
+}
+
+/* ncalls x multistep_2MN_gauge (md_integrator.c:347-376): a pure-gauge
+ * trajectory is 2 no_md of them (the fermion kicks of
+ * multistep_2MN_SOLOOPENACC vanish without fermions) */
+void ref_2mn_gauge(double *u, double *mom, double beta, int no_md, int gauge_scale, double t, int ncalls)
+{
+  double d7[7];
+  ref_md_deltas(beta, no_md, gauge_scale, t, d7);
+  su3_soa *stap = xalloc(8 * sizeof(su3_soa));
+  tamat_soa *ip = xalloc(8 * sizeof(tamat_soa));
+  for (int k = 0; k < ncalls; k++)
+    multistep_2MN_gauge((su3_soa *)u, stap, ip, (thmat_soa *)mom);
+  free(stap); free(ip);
 }

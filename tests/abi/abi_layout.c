@@ -1,11 +1,12 @@
 /* abi_layout.c -- prints the size and field offsets of the plain structs
  * that cross the C ABI (RationalApprox, ferm_param, inv_tricks,
- * inverter_package, action_param) and the element sizes of the SoA types.
+ * inverter_package, action_param, md_param) and the element sizes of the SoA types.
  *
  * Built twice by tests/test_abi_reference.py:
  *   -DWITH_REFERENCE_HEADERS: with the reference's own headers
  *      (struct_c_def.h, fermion_parameters.h, inverter_package.h, action.h,
- *      rationalapprox.h, inverter_tricks.h and the hot-path function headers)
+ *      rationalapprox.h, inverter_tricks.h, md_parameters.h and the hot-path
+ *      and gauge-HMC function headers)
  *      included BEFORE ostaple_gb300.h with OSTAPLE_HAVE_REFERENCE_TYPES, so
  *      the compiler also checks that every prototype the library declares is
  *      compatible with the reference's declaration of the same function;
@@ -32,6 +33,14 @@
 #include "fermion_force_utilities.h"
 #include "find_min_max.h"
 #include "float_double_conv.h"
+#include "ipdot_gauge.h"
+#include "plaquettes.h"
+#include "rectangles.h"
+#include "su3_utilities.h"
+#include "su3_measurements.h"
+#include "md_parameters.h"
+#include "md_integrator.h"
+#include "random_assignement.h"
 #define OSTAPLE_HAVE_REFERENCE_TYPES
 #endif
 #include "ostaple_gb300.h"
@@ -58,6 +67,10 @@ int main(void)
   F(inverter_package, u); F(inverter_package, u_f); F(inverter_package, ferm_shift_temp);
   F(inverter_package, ferm_shift_temp_f); F(inverter_package, nshifts); F(inverter_package, loc_r);
   F(inverter_package, loc_p); F(inverter_package, loc_r_f); F(inverter_package, loc_p_f); F(inverter_package, out_f);
+  printf("md_param %zu\n", sizeof(md_param));
+  F(md_param, no_md); F(md_param, gauge_scale); F(md_param, t); F(md_param, residue_metro);
+  F(md_param, expected_max_eigenvalue); F(md_param, singlePrecMD); F(md_param, residue_md);
+  F(md_param, max_cg_iterations); F(md_param, recycleInvsForce); F(md_param, extrapolateInvsForce);
   printf("action_param %zu\n", sizeof(action_param));
   F(action_param, beta); F(action_param, stout_steps); F(action_param, stout_rho); F(action_param, topo_action);
   F(action_param, barrier); F(action_param, width); F(action_param, topo_file_path);

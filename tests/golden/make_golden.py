@@ -7,7 +7,7 @@ Run from the repository root where the reference source tree is available
 (its path as the first argument, or in OSTAPLE_REFERENCE), optionally naming
 the fixture groups to write (default: all):
 
-    python tests/golden/make_golden.py /path/to/reference [dirac] [gauge] [config2]
+    python tests/golden/make_golden.py /path/to/reference [dirac] [gauge] [config2] [hmc]
 
 * dirac   -- dirac_<dims>.npz: D_eo/D_oe, M^+M, CG, CG-M, eigenvalue bounds;
 * gauge   -- gauge_<dims>_e<eps>.npz: staples, Q_A, stout levels,
@@ -15,7 +15,10 @@ the fixture groups to write (default: all):
   steps and a whole fermion_force_soloopenacc with two pseudofermions;
 * config2 -- config2_16x16x16x16.npz: the 16^4 benchmark configuration
   (2 stout steps of rho = 0.15, m = 0.05, order-8 CG-M to 1e-10 per shift,
-  the rational fermion force), at sampled sites.
+  the rational fermion force), at sampled sites;
+* hmc     -- hmc_<dims>.npz: the pure-gauge tree-level Symanzik HMC pieces
+  (gauge staples and force, plaquette and rectangle sums, 1/2 tr P^2, the
+  momentum kick, the link update, two multistep_2MN_gauge calls).
 
 Inputs are regenerated from seeds by openstaple_gb300.fields, whose
 counter-based generator is platform independent; the fixture also stores a
@@ -215,6 +218,44 @@ def write_config2(approx: dict) -> None:
     print("wrote config2: cgm", n, "iterations, status", st)
 
 
+# pure-gauge tree-level Symanzik HMC pieces: (dims, link seed, eps, stride)
+HMC_CASES = [((4, 4, 4, 4), 501, 0.5, 1), ((4, 6, 8, 10), 502, 0.3, 15)]
+HMC_MOM = (61, 3)                       # momenta (seed, stream) of fields.gauge_momenta
+HMC_MD = dict(beta=3.75, no_md=3, gauge_scale=2, t=1.0, ncalls=2)
+
+
+def write_hmc(approx: dict) -> None:
+    build.build_reference_oracles(sorted({c[0] for c in HMC_CASES}))
+    for dims, sl, eps, stride in HMC_CASES:
+        r = Reference(dims)
+        u = F.random_su3_links(dims, sl, eps=eps)
+        mom = F.gauge_momenta(dims, *HMC_MOM)
+        sites = np.arange(0, r.sizeh, stride)
+        aidx = alg_index(r.sizeh, sites)
+
+        def smp(f):
+            return np.ascontiguousarray(f[..., sites])
+
+        def smp_alg(f):
+            return np.ascontiguousarray(f[:, aidx])
+
+        ip = r.ipdot_gauge(u)
+        md = HMC_MD
+        u2, m2 = r.gauge_2mn(u, mom, md["beta"], md["no_md"], md["gauge_scale"], md["t"], md["ncalls"])
+        out = dict(dims=np.array(dims), link_seed=sl, eps=eps, stride=stride, sites=sites, alg_idx=aidx,
+                   mom_seed=HMC_MOM[0], mom_stream=HMC_MOM[1], u_checksum=checksum(u),
+                   mom_checksum=float(np.sum(mom ** 2)),
+                   staples=smp(r.gauge_staples(u)), ipdot=smp_alg(ip),
+                   plaq_sum=r.plaquette_sum(u), rect_sum=r.rectangle_sum(u), mom_action=r.momenta_action(mom),
+                   mom_sum_mult=smp_alg(r.mom_sum_mult(mom, ip, -0.02)),
+                   mom_exp=smp(r.mom_exp_times_conf(u, mom, 0.05)[:, :2]),
+                   deltas=r.md_deltas(md["beta"], md["no_md"], md["gauge_scale"], md["t"]),
+                   md_u=smp(u2[:, :2]), md_mom=smp_alg(m2), **{f"md_{k}": v for k, v in md.items()})
+        tag = "x".join(map(str, dims))
+        np.savez_compressed(HERE / f"hmc_{tag}.npz", **out)
+        print("wrote hmc", tag)
+
+
 def main(refroot: str, groups) -> None:
     ref = Path(refroot)
     os.environ["OSTAPLE_REFERENCE"] = str(ref)
@@ -226,12 +267,14 @@ def main(refroot: str, groups) -> None:
         write_gauge(approx)
     if "config2" in groups:
         write_config2(approx)
+    if "hmc" in groups:
+        write_hmc(approx)
 
 
 if __name__ == "__main__":
     args = sys.argv[1:]
-    root = args.pop(0) if args and not args[0] in ("dirac", "gauge", "config2") else os.environ.get(
+    root = args.pop(0) if args and not args[0] in ("dirac", "gauge", "config2", "hmc") else os.environ.get(
         "OSTAPLE_REFERENCE")
     if not root:
-        sys.exit("usage: make_golden.py /path/to/reference [dirac] [gauge] [config2]")
-    main(root, set(args) or {"dirac", "gauge", "config2"})
+        sys.exit("usage: make_golden.py /path/to/reference [dirac] [gauge] [config2] [hmc]")
+    main(root, set(args) or {"dirac", "gauge", "config2", "hmc"})

@@ -272,3 +272,70 @@ def test_oracle_matches_golden_config2(built):
     assert relerr(_smp(o.recombine(xs, phi, float(g["a0"]), g["a"]), g), g["recombined"]) <= 1e-12
     ip = _oracle_force(o, u, ph, mass, g["a"], g["b"], phi[None], res, rho)
     assert relerr(_smp_alg(ip, g), g["fermion_force"]) <= 1e-11
+
+
+# ---- pure-gauge tree-level Symanzik HMC ------------------------------------
+# Tolerances: 1e-14 relative (max-norm) for the staples, the force, the
+# momentum kick and the link update; 1e-13 relative for the plaquette,
+# rectangle and momentum sums; 1e-12 after two gauge multisteps (18 force
+# evaluations and link updates in sequence).
+
+HMC_TAGS = ["4x4x4x4", "4x6x8x10"]
+
+
+def _hmc_fixture(tag):
+    from conftest import GOLDEN
+    g = dict(np.load(GOLDEN / f"hmc_{tag}.npz"))
+    dims = tuple(int(d) for d in g["dims"])
+    u = F.random_su3_links(dims, int(g["link_seed"]), eps=float(g["eps"]))
+    mom = F.gauge_momenta(dims, int(g["mom_seed"]), int(g["mom_stream"]))
+    assert np.isclose(np.sum(np.abs(u) ** 2), float(g["u_checksum"]), rtol=1e-14)
+    assert np.isclose(np.sum(mom ** 2), float(g["mom_checksum"]), rtol=1e-14)
+    return g, dims, u, mom
+
+
+@pytest.mark.parametrize("dims", REF_DIMS)
+def test_oracle_gauge_hmc_matches_compiled_reference(built, dims):
+    """Staples and force of the tree-level Symanzik action, plaquette and
+    rectangle sums, 1/2 tr P^2, the momentum kick, the link update and two
+    gauge multisteps of the 2MN integrator: the oracle against the
+    reference's own compiled ipdot_gauge.c, plaquettes.c, rectangles.c,
+    su3_utilities.c, su3_measurements.c, md_integrator.c, md_parameters.c."""
+    from oracle import Oracle, Reference, ref_available
+    if not ref_available(dims):
+        pytest.skip("reference not compiled here (no reference source tree)")
+    r, o = Reference(dims), Oracle(dims)
+    u = F.random_su3_links(dims, 601, eps=0.4)
+    mom = F.gauge_momenta(dims, 602, 1)
+    assert relerr(o.gauge_staples(u), r.gauge_staples(u)) <= 1e-14
+    ip = r.ipdot_gauge(u)
+    assert relerr(o.ipdot_gauge(u), ip) <= 1e-14
+    assert abs(o.plaquette_sum(u) - r.plaquette_sum(u)) <= 1e-13 * abs(r.plaquette_sum(u))
+    assert abs(o.rectangle_sum(u) - r.rectangle_sum(u)) <= 1e-13 * abs(r.rectangle_sum(u))
+    assert abs(o.momenta_action(mom) - r.momenta_action(mom)) <= 1e-13 * r.momenta_action(mom)
+    assert relerr(o.mom_sum_mult(mom, ip, -0.03), r.mom_sum_mult(mom, ip, -0.03)) <= 1e-14
+    assert relerr(o.mom_exp_times_conf(u, mom, 0.05)[:, :2], r.mom_exp_times_conf(u, mom, 0.05)[:, :2]) <= 1e-14
+    assert np.array_equal(o.md_deltas(3.75, 18, 4, 1.0), r.md_deltas(3.75, 18, 4, 1.0))
+    uo, mo = o.gauge_2mn(u, mom, 3.75, 2, 3, 1.0, 2)
+    ur, mr = r.gauge_2mn(u, mom, 3.75, 2, 3, 1.0, 2)
+    assert relerr(uo[:, :2], ur[:, :2]) <= 1e-12
+    assert relerr(mo, mr) <= 1e-12
+
+
+@pytest.mark.parametrize("tag", HMC_TAGS)
+def test_oracle_matches_golden_hmc(built, tag):
+    from oracle import Oracle
+    g, dims, u, mom = _hmc_fixture(tag)
+    o = Oracle(dims)
+    ip = o.ipdot_gauge(u)
+    assert relerr(_smp(o.gauge_staples(u), g), g["staples"]) <= 1e-14
+    assert relerr(_smp_alg(ip, g), g["ipdot"]) <= 1e-14
+    assert abs(o.plaquette_sum(u) - float(g["plaq_sum"])) <= 1e-13 * abs(float(g["plaq_sum"]))
+    assert abs(o.rectangle_sum(u) - float(g["rect_sum"])) <= 1e-13 * abs(float(g["rect_sum"]))
+    assert abs(o.momenta_action(mom) - float(g["mom_action"])) <= 1e-13 * float(g["mom_action"])
+    assert relerr(_smp_alg(o.mom_sum_mult(mom, ip, -0.02), g), g["mom_sum_mult"]) <= 1e-14
+    assert relerr(_smp(o.mom_exp_times_conf(u, mom, 0.05)[:, :2], g), g["mom_exp"]) <= 1e-14
+    uo, mo = o.gauge_2mn(u, mom, float(g["md_beta"]), int(g["md_no_md"]), int(g["md_gauge_scale"]),
+                         float(g["md_t"]), int(g["md_ncalls"]))
+    assert relerr(_smp(uo[:, :2], g), g["md_u"]) <= 1e-12
+    assert relerr(_smp_alg(mo, g), g["md_mom"]) <= 1e-12
