@@ -512,6 +512,31 @@ int ostaple_gauge_momenta(thmat_soa *mom, unsigned long long seed, unsigned long
 /* plaquette and rectangle sums and the action -beta/3 (C_ZERO P + C_ONE R) */
 int ostaple_gauge_action(const su3_soa *u, double beta, double *plaq_sum, double *rect_sum, double *action);
 
+/* ---- RHMC trajectory ------------------------------------------------------ */
+/* the molecular dynamics with fermions (md_integrator.h:17-32):
+ *   F(d0) [G F(d1) G F(d2)]^(no_md-1) G F(d1) G F(d0)
+ * with F the fermion force of all flavours (fermion_force_soloopenacc, then
+ * mom_sum_mult) and G multistep_2MN_gauge; steps from deltas_Omelyan and
+ * md_parameters.  local_sums is not used. */
+void multistep_2MN_SOLOOPENACC(tamat_soa *tipdot_acc, su3_soa *tconf_acc, su3_soa *tstout_conf_acc_arr,
+                               su3_soa *tauxbis_conf_acc, su3_soa *taux_conf_acc, ferm_param *tfermions_parameters,
+                               int tNDiffFlavs, vec3_soa *ferm_in_acc, vec3_soa *tferm_shiftmulti_acc,
+                               inverter_package ip, thmat_soa *tmomenta, dcomplex_soa *local_sums, double res,
+                               const int max_cg);
+/* One RHMC update with explicit arguments (the reference's
+ * UPDATE_SOLOACC_UNOSTEP_VERSATILE, update_versatile.c:44-665, reads them
+ * from its globals): Gaussian momenta and pseudofermions phi from the
+ * counter-based generator (seed, traj); eigenvalue bounds of M^+M on the
+ * smeared links and approx_fi/md/li rescaled from the mothers in fpars;
+ * chi = r_fi phi; 2MN molecular dynamics of no_md steps x gauge_scale
+ * substeps over traj_len with beta; phi' = r_li chi; Metropolis on
+ * dS = dH (when metropolis != 0; a rejected update restores u).  Solvers
+ * follow inverter_tricks.  action[6] (may be NULL): -S_gauge, S_mom, S_ferm
+ * before, then after.  No reference counterpart as a function. */
+int ostaple_rhmc_trajectory(su3_soa *u, ferm_param *fpars, int nflavs, double beta, int no_md, int gauge_scale,
+                            double traj_len, double res_metro, double res_md, int max_cg, unsigned long long seed,
+                            int traj, int metropolis, int *accepted, double *delta_s, double *action);
+
 /* Mixed-precision CG that iterates until the FP64 true residual
  * sqrt(|b - (M^+M + shift) x|^2 / |b|^2) is <= res (or max_iter), with a
  * reliable update every `reliable_every` iterations, or (reliable_every = 0)

@@ -346,6 +346,20 @@ def pure_gauge_hmc(u, beta: float, ntraj: int, no_md: int = 18, gauge_scale: int
     return dict(accepted=acc.value, plaquette=plaq[:ntraj], delta_s=ds[:ntraj])
 
 
+def rhmc_trajectory(u, fpars, beta: float, no_md: int, gauge_scale: int, traj_len: float = 1.0,
+                    res_metro: float = 1e-10, res_md: float = 1e-8, max_cg: int = 10000, seed: int = 1, traj: int = 0,
+                    metropolis: bool = True) -> dict:
+    """One RHMC update of the links u (device-resident) with the flavours
+    fpars (a ctypes array of FermParam with their mother approximations)."""
+    acc, ds = C.c_int(0), C.c_double(0)
+    act = np.zeros(6)
+    rc = lib().ostaple_rhmc_trajectory(ptr(u), fpars, len(fpars), beta, no_md, gauge_scale, traj_len, res_metro, res_md,
+                                       max_cg, seed, traj, int(metropolis), C.byref(acc), C.byref(ds),
+                                       act.ctypes.data)
+    check(rc, "ostaple_rhmc_trajectory")
+    return dict(accepted=acc.value, delta_s=ds.value, action=act)
+
+
 def gauge_momenta(mom, seed: int, stream: int) -> None:
     check(lib().ostaple_gauge_momenta(ptr(mom), seed, stream), "ostaple_gauge_momenta")
 

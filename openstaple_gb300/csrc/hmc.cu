@@ -583,6 +583,28 @@ void launch_gen_momenta(R* mom, unsigned long long seed, unsigned long long stre
   OST_LAUNCH_CHECK();
 }
 
+// Gaussian complex 3-vectors (vec3_soa over sizeh sites): element k of the
+// 3*sizeh complex numbers takes the Box-Muller pair k of (seed, stream), as
+// the host field helpers' gaussian_vec3 (the reference's
+// generate_vec3_soa_gauss, random_assignement.c:58-92: real and imaginary
+// parts of variance 1/2)
+__global__ void k_gen_vec3(double2* v, long n, unsigned long long seed, unsigned long long stream) {
+  const long k = blockIdx.x * long(blockDim.x) + threadIdx.x;
+  if (k >= n) return;
+  const double u1 = uniform01(seed, 2 * stream, (unsigned long long)k);
+  const double u2 = uniform01(seed, 2 * stream + 1, (unsigned long long)k);
+  const double rad = sqrt(-log(u1));
+  double sn, cs;
+  sincospi(2.0 * u2, &sn, &cs);
+  v[k] = make_double2(rad * cs, rad * sn);
+}
+
+void launch_gen_vec3_gauss(double2* v, unsigned long long seed, unsigned long long stream, cudaStream_t st) {
+  const long n = 3L * rt().g.sizeh;
+  k_gen_vec3<<<int((n + 255) / 256), 256, 0, st>>>(v, n, seed, stream);
+  OST_LAUNCH_CHECK();
+}
+
 // ---- precision conversions of the link generator ----
 __global__ void k_links_64_to_32(const double2* __restrict__ u64, int rows64, float2* u32, long sh) {
   const long t = blockIdx.x * long(blockDim.x) + threadIdx.x;

@@ -52,6 +52,9 @@ void launch_momenta_action(const R* mom, int d0, int d1, double* dst, cudaStream
 // (random_assignement.c:145-185)
 template <typename R>
 void launch_gen_momenta(R* mom, unsigned long long seed, unsigned long long stream, cudaStream_t st);
+// Gaussian vec3_soa (3*sizeh complex numbers, real and imaginary parts of
+// variance 1/2) from the same generator
+void launch_gen_vec3_gauss(double2* v, unsigned long long seed, unsigned long long stream, cudaStream_t st);
 // FP64 reference-layout links <-> compact two-row FP32 links; the way back
 // reunitarises rows 0-1 in FP64
 void launch_links_64_to_32(const double2* u64, int rows64, float2* u32, cudaStream_t st);

@@ -108,6 +108,7 @@ enum WorkspaceSlot {
   WS_HMC_MOM,      // link generator: FP64 momenta
   WS_HMC_BKP,      // link generator: links before the trajectory (Metropolis reject)
   WS_HMC_F32,      // link generator: FP32 links and momenta of the molecular dynamics
+  WS_RHMC,         // RHMC trajectory: smeared levels, parking fields, pseudofermions, momenta
   WS_NSLOTS
 };
 

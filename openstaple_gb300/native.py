@@ -199,6 +199,10 @@ SIGNATURES = {
     "ostaple_pure_gauge_hmc": (_I, [_P, _D, _I, _I, _I, _D, C.c_ulonglong, _I, _I, _I, C.POINTER(_I), _P, _P]),
     "ostaple_gauge_momenta": (_I, [_P, C.c_ulonglong, C.c_ulonglong]),
     "ostaple_gauge_action": (_I, [_P, _D, C.POINTER(_D), C.POINTER(_D), C.POINTER(_D)]),
+    "multistep_2MN_SOLOOPENACC": (None, [_P, _P, _P, _P, _P, C.POINTER(FermParam), _I, _P, _P, InverterPackage, _P, _P,
+                                         _D, _I]),
+    "ostaple_rhmc_trajectory": (_I, [_P, C.POINTER(FermParam), _I, _D, _I, _I, _D, _D, _D, _I, C.c_ulonglong, _I,
+                                     _I, C.POINTER(_I), C.POINTER(_D), _P]),
     # single-precision twins (sp_*.c) and float <-> double conversions
     "acc_Deo_f": (None, [_P, _P, _P, _P]),
     "acc_Doe_f": (None, [_P, _P, _P, _P]),

@@ -292,6 +292,7 @@ class Reference:
         "ref_mom_exp_times_conf": (None, [_P, _P, _D]),
         "ref_md_deltas": (None, [_D, _I, _I, _D, _P]),
         "ref_2mn_gauge": (None, [_P, _P, _D, _I, _I, _D, _I]),
+        "ref_rhmc_md": (None, [_P, _P, _P, _D, _I, _I, _P, _P, _P, _D, _I, _D, _I, _I, _D, _I, _D]),
     }
 
     def __init__(self, dims):
@@ -481,3 +482,15 @@ class Reference:
         st = self.su3()
         self.L.ref_ipdot_gauge(_p(u), _p(st), _p(ip))
         return ip
+
+    def rhmc_md(self, u, mom, ph, mass, a, b, chis, res, beta, no_md, gauge_scale, t, steps=2, rho=0.15,
+                max_cg=10000):
+        """(U, P) after the reference's multistep_2MN_SOLOOPENACC with one
+        flavour of len(chis) pseudofermions and approx_md = (a, b)."""
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        chis = np.ascontiguousarray(chis, dtype=np.complex128).reshape(-1, 3, self.sizeh)
+        uo, mo = u.copy(), np.ascontiguousarray(mom).copy()
+        self.L.ref_rhmc_md(_p(uo), _p(mo), _p(np.ascontiguousarray(ph)), mass, len(chis), len(a), _p(a), _p(b),
+                           _p(chis), res, max_cg, beta, no_md, gauge_scale, t, steps, rho)
+        return uo, mo

@@ -477,3 +477,48 @@ void ref_2mn_gauge(double *u, double *mom, double beta, int no_md, int gauge_sca
     multistep_2MN_gauge((su3_soa *)u, stap, ip, (thmat_soa *)mom);
   free(stap); free(ip);
 }
+
+/* ---- molecular dynamics with fermions: the reference's
+ * multistep_2MN_SOLOOPENACC (md_integrator.c:502-742) for one flavour of
+ * nps pseudofermions chi[nps] with approx_md = (a, b), mass, stout (steps,
+ * rho), gauge action beta, integrator (no_md, gauge_scale, t).  u and mom
+ * are updated in place. ---- */
+void ref_rhmc_md(double *u, double *mom, double *ph, double mass, int nps, int order, const double *a,
+                 const double *b, const double *chi, double res, int max_cg, double beta, int no_md,
+                 int gauge_scale, double t, int steps, double rho)
+{
+  size_t vb = sizeof(vec3_soa);
+  act_params.stout_steps = steps;
+  act_params.topo_action = 0;
+  gl_stout_rho = rho;
+  double d7[7];
+  ref_md_deltas(beta, no_md, gauge_scale, t, d7);
+  alloc_info.maxNeededShifts = order;
+  alloc_info.NDiffFlavs = 1;
+  aux_th = xalloc(8 * sizeof(thmat_soa));
+  aux_ta = xalloc(8 * sizeof(tamat_soa));
+  stout_globals(1);
+  su3_soa *levels = xalloc(8 * (size_t)(steps > 0 ? steps : 1) * sizeof(su3_soa));
+  su3_soa *auxbis = xalloc(8 * sizeof(su3_soa)), *aux = xalloc(8 * sizeof(su3_soa));
+  tamat_soa *ipdot = xalloc(8 * sizeof(tamat_soa));
+  vec3_soa *shiftmulti = xalloc(vb * (size_t)order), *shifttemp = xalloc(vb * (size_t)order);
+  vec3_soa *r = xalloc(vb), *h = xalloc(vb), *s = xalloc(vb), *p = xalloc(vb);
+  dcomplex_soa *sums = xalloc(2 * sizeof(dcomplex_soa));
+  ferm_param fp; make_fp(&fp, ph, mass);
+  fp.number_of_ps = nps;
+  fp.index_of_the_first_ps = 0;
+  fp.approx_md.approx_order = order;
+  for (int i = 0; i < order; i++) { fp.approx_md.RA_a[i] = a[i]; fp.approx_md.RA_b[i] = b[i]; }
+  inverter_package ip;
+  memset(&ip, 0, sizeof(ip));
+  ip.u = (const su3_soa *)u;
+  ip.ferm_shift_temp = shifttemp; ip.nshifts = order;
+  ip.loc_r = r; ip.loc_h = h; ip.loc_s = s; ip.loc_p = p;
+  multistep_2MN_SOLOOPENACC(ipdot, (su3_soa *)u, levels, auxbis, aux, &fp, 1, (vec3_soa *)chi, shiftmulti, ip,
+                            (thmat_soa *)mom, sums, res, max_cg);
+  free(levels); free(auxbis); free(aux); free(ipdot); free(shiftmulti); free(shifttemp);
+  free(r); free(h); free(s); free(p); free(sums);
+  free(aux_th); free(aux_ta);
+  aux_th = NULL; aux_ta = NULL;
+  stout_globals(0);
+}

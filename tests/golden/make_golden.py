@@ -7,7 +7,7 @@ Run from the repository root where the reference source tree is available
 (its path as the first argument, or in OSTAPLE_REFERENCE), optionally naming
 the fixture groups to write (default: all):
 
-    python tests/golden/make_golden.py /path/to/reference [dirac] [gauge] [config2] [hmc]
+    python tests/golden/make_golden.py /path/to/reference [dirac] [gauge] [config2] [hmc] [rhmc]
 
 * dirac   -- dirac_<dims>.npz: D_eo/D_oe, M^+M, CG, CG-M, eigenvalue bounds;
 * gauge   -- gauge_<dims>_e<eps>.npz: staples, Q_A, stout levels,
@@ -18,7 +18,9 @@ the fixture groups to write (default: all):
   the rational fermion force), at sampled sites;
 * hmc     -- hmc_<dims>.npz: the pure-gauge tree-level Symanzik HMC pieces
   (gauge staples and force, plaquette and rectangle sums, 1/2 tr P^2, the
-  momentum kick, the link update, two multistep_2MN_gauge calls).
+  momentum kick, the link update, two multistep_2MN_gauge calls);
+* rhmc    -- rhmc_md_4x4x4x4.npz: the reference's multistep_2MN_SOLOOPENACC
+  (molecular dynamics with a two-pseudofermion flavour and stout smearing).
 
 Inputs are regenerated from seeds by openstaple_gb300.fields, whose
 counter-based generator is platform independent; the fixture also stores a
@@ -47,6 +49,7 @@ CASES = [((4, 4, 4, 4), 11, 5, 0.1), ((4, 6, 8, 10), 12, 6, 0.05), ((8, 8, 8, 8)
 APPROX_FILES = {
     "order8": "tools/test/ratapproxes/approx_-1_over_4_mlogerr_3.8_mloglm_6.2.REMEZ",
     "order19": "saved_approxs/approx_-1_over_4_order_19_mloglm_6.4.REMEZ",
+    "fi_1_over_8": "tools/test/ratapproxes/approx_1_over_8_mlogerr_8.1_mloglm_6.2.REMEZ",
 }
 
 
@@ -256,6 +259,31 @@ def write_hmc(approx: dict) -> None:
         print("wrote hmc", tag)
 
 
+# molecular dynamics with fermions: one flavour, two pseudofermions chi,
+# order-8 x^(-1/4) approx_md, stout 2 x 0.15
+RHMC_MD = dict(dims=(4, 4, 4, 4), link_seed=701, eps=0.3, mom=(702, 0), chi_seeds=(703, 704), mass=0.1, res=1e-12,
+               beta=3.75, no_md=2, gauge_scale=2, t=1.0, steps=2, rho=0.15)
+
+
+def write_rhmc(approx: dict) -> None:
+    c = RHMC_MD
+    dims = c["dims"]
+    build.build_reference_oracles([dims])
+    r = Reference(dims)
+    ph = r.phases()
+    u = F.random_su3_links(dims, c["link_seed"], eps=c["eps"])
+    mom = F.gauge_momenta(dims, *c["mom"])
+    chis = np.stack([F.gaussian_vec3(dims, k) for k in c["chi_seeds"]])
+    a0, a, b = approx_rescaled(approx, "order8")
+    ur, mr = r.rhmc_md(u, mom, ph, c["mass"], a, b, chis, c["res"], c["beta"], c["no_md"], c["gauge_scale"], c["t"],
+                       c["steps"], c["rho"])
+    out = dict(u_checksum=checksum(u), mom_checksum=float(np.sum(mom ** 2)), chi_checksum=checksum(chis),
+               a=a, b=b, md_u=np.ascontiguousarray(ur[:, :2]), md_mom=mr)
+    out.update({k: np.array(v) for k, v in c.items()})
+    np.savez_compressed(HERE / "rhmc_md_4x4x4x4.npz", **out)
+    print("wrote rhmc md")
+
+
 def main(refroot: str, groups) -> None:
     ref = Path(refroot)
     os.environ["OSTAPLE_REFERENCE"] = str(ref)
@@ -269,12 +297,14 @@ def main(refroot: str, groups) -> None:
         write_config2(approx)
     if "hmc" in groups:
         write_hmc(approx)
+    if "rhmc" in groups:
+        write_rhmc(approx)
 
 
 if __name__ == "__main__":
     args = sys.argv[1:]
-    root = args.pop(0) if args and not args[0] in ("dirac", "gauge", "config2", "hmc") else os.environ.get(
+    root = args.pop(0) if args and not args[0] in ("dirac", "gauge", "config2", "hmc", "rhmc") else os.environ.get(
         "OSTAPLE_REFERENCE")
     if not root:
-        sys.exit("usage: make_golden.py /path/to/reference [dirac] [gauge] [config2] [hmc]")
-    main(root, set(args) or {"dirac", "gauge", "config2", "hmc"})
+        sys.exit("usage: make_golden.py /path/to/reference [dirac] [gauge] [config2] [hmc] [rhmc]")
+    main(root, set(args) or {"dirac", "gauge", "config2", "hmc", "rhmc"})

@@ -339,3 +339,42 @@ def test_oracle_matches_golden_hmc(built, tag):
                          float(g["md_t"]), int(g["md_ncalls"]))
     assert relerr(_smp(uo[:, :2], g), g["md_u"]) <= 1e-12
     assert relerr(_smp_alg(mo, g), g["md_mom"]) <= 1e-12
+
+
+def test_oracle_fermion_md_matches_golden(built):
+    """The reference's multistep_2MN_SOLOOPENACC (molecular dynamics with a
+    two-pseudofermion flavour, stout 2 x 0.15) restated from oracle pieces:
+    F(d0) [G F(d1) G F(d2)]^(no_md-1) G F(d1) G F(d0), F the fermion force
+    kick and G one gauge multistep (md_integrator.c:502-742).  Links and
+    momenta within 1e-12."""
+    from conftest import GOLDEN
+    from oracle import Oracle
+    g = dict(np.load(GOLDEN / "rhmc_md_4x4x4x4.npz"))
+    dims = tuple(int(d) for d in g["dims"])
+    o = Oracle(dims)
+    u = F.random_su3_links(dims, int(g["link_seed"]), eps=float(g["eps"]))
+    mom = F.gauge_momenta(dims, *[int(v) for v in g["mom"]])
+    chis = np.stack([F.gaussian_vec3(dims, int(k)) for k in g["chi_seeds"]])
+    ph = o.phases()
+    beta, no_md, gs, t = float(g["beta"]), int(g["no_md"]), int(g["gauge_scale"]), float(g["t"])
+    d = o.md_deltas(beta, no_md, gs, t)
+    mass, res, rho = float(g["mass"]), float(g["res"]), float(g["rho"])
+
+    def F_(uu, mm, k):
+        return o.mom_sum_mult(mm, _oracle_force(o, uu, ph, mass, g["a"], g["b"], chis, res, rho), d[k])
+
+    def G_(uu, mm):
+        return o.gauge_2mn(uu, mm, beta, no_md, gs, t, 1)
+
+    mom = F_(u, mom, 0)
+    for _ in range(1, no_md):
+        u, mom = G_(u, mom)
+        mom = F_(u, mom, 1)
+        u, mom = G_(u, mom)
+        mom = F_(u, mom, 2)
+    u, mom = G_(u, mom)
+    mom = F_(u, mom, 1)
+    u, mom = G_(u, mom)
+    mom = F_(u, mom, 0)
+    assert relerr(u[:, :2], g["md_u"]) <= 1e-12
+    assert relerr(mom, g["md_mom"]) <= 1e-12
