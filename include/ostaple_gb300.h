@@ -45,6 +45,7 @@ typedef struct vec3_soa_f_t vec3_soa_f;   /* float twins (generated sp_ types) *
 typedef struct su3_soa_f_t su3_soa_f;
 typedef struct float_soa_t float_soa;
 typedef struct dcomplex_soa_t dcomplex_soa; /* c[sizeh] double complex     */
+typedef struct global_su3_soa_t global_su3_soa; /* su3_soa of the whole lattice */
 
 #define INVERTER_SUCCESS 1                /* inverter_full.h:12 */
 #define INVERTER_FAILURE 0                /* inverter_full.h:13 */
@@ -536,6 +537,27 @@ void multistep_2MN_SOLOOPENACC(tamat_soa *tipdot_acc, su3_soa *tconf_acc, su3_so
 int ostaple_rhmc_trajectory(su3_soa *u, ferm_param *fpars, int nflavs, double beta, int no_md, int gauge_scale,
                             double traj_len, double res_metro, double res_md, int max_cg, unsigned long long seed,
                             int traj, int metropolis, int *accepted, double *delta_s, double *action);
+
+/* ---- configuration files (io.h:17-89; host memory, no GPU needed) ---------
+ * On one process the global lattice is the local one: conf is a host
+ * su3_soa[8] of the lattice given to ostaple_init.  ASCII: a header line
+ * "nx ny nz nt beta mass nflavs traj" (beta from act_params; mass and the
+ * flavour count from ostaple_io_ferm_mass / ostaple_io_nflavs, 0 by
+ * default), then every link as 3 rows of "(re, im)" pairs printed %.18lf, in
+ * the order direction 2*mu+parity, half-lattice index; with back_phases the
+ * links are written times the sign of their staggered phase, and reading
+ * undoes a determinant of -1.  ILDG: LIME records "ildg-format" (XML with
+ * lx..lt), "MD_traj", "input-file" (input_file_str), "ildg-binary-data"
+ * (big-endian doubles, t z y x with x fastest, directions x y z t, 3x3
+ * row-major complex) and "ildg-data-lfn".  Return 0 on success, 1 when the
+ * file cannot be opened for reading, 2 on other errors. */
+int print_su3_soa_ASCII(global_su3_soa *const conf, const char *nomefile, int conf_id_iter, double_soa *back_phases);
+int read_su3_soa_ASCII(global_su3_soa *conf, const char *nomefile, int *conf_id_iter);
+int print_su3_soa_ildg_binary(global_su3_soa *conf, const char *nomefile, int conf_id_iter);
+int read_su3_soa_ildg_binary(global_su3_soa *conf, const char *nomefile, int *conf_id_iter);
+extern char input_file_str[300 * 500];        /* setting_file_parser.h:11 */
+extern double ostaple_io_ferm_mass;            /* no reference counterpart */
+extern int ostaple_io_nflavs;                  /* no reference counterpart */
 
 /* Mixed-precision CG that iterates until the FP64 true residual
  * sqrt(|b - (M^+M + shift) x|^2 / |b|^2) is <= res (or max_iter), with a

@@ -16,6 +16,7 @@
 namespace ost {
 
 static Runtime g_rt;
+static Geom g_host_geom{};
 unsigned long long g_kernel_launches = 0;
 
 bool pdl_enabled() {
@@ -27,6 +28,7 @@ bool pdl_enabled() {
   return on == 1;
 }
 Runtime& rt() { return g_rt; }
+const Geom& host_geom() { return g_host_geom; }
 
 static int g_err = 0;
 static char g_msg[512] = "";
@@ -132,6 +134,13 @@ int ostaple_init(int n0, int n1, int n2, int n3) {
     set_error(-6, "ostaple_init: lattice too large");
     return -6;
   }
+  // the lattice is known to the host-only functions (configuration files)
+  // even when no device can be initialised
+  g_host_geom = Geom{};
+  g_host_geom.n0 = n0; g_host_geom.n1 = n1; g_host_geom.n2 = n2; g_host_geom.n3 = n3;
+  g_host_geom.nh0 = n0 / 2;
+  g_host_geom.sizeh = int(vol / 2);
+  g_host_geom.vol1 = n0; g_host_geom.vol2 = n0 * n1; g_host_geom.vol3 = n0 * n1 * n2;
   Runtime& r = g_rt;
   if (!r.initialized) {
     if (cudaGetDevice(&r.device) != cudaSuccess) { cudaGetLastError(); r.device = 0; }

@@ -18,6 +18,10 @@ struct Runtime {
 };
 
 Runtime& rt();
+// The lattice of the last ostaple_init call with valid extents, also when no
+// device could be initialised (host-only functions such as the configuration
+// files use it).
+const Geom& host_geom();
 
 // Error state: the reference's void entry points report through printf; this
 // library records the first failure and returns failure codes where the

@@ -203,6 +203,11 @@ SIGNATURES = {
                                          _D, _I]),
     "ostaple_rhmc_trajectory": (_I, [_P, C.POINTER(FermParam), _I, _D, _I, _I, _D, _D, _D, _I, C.c_ulonglong, _I,
                                      _I, C.POINTER(_I), C.POINTER(_D), _P]),
+    # configuration files
+    "print_su3_soa_ASCII": (_I, [_P, C.c_char_p, _I, _P]),
+    "read_su3_soa_ASCII": (_I, [_P, C.c_char_p, C.POINTER(_I)]),
+    "print_su3_soa_ildg_binary": (_I, [_P, C.c_char_p, _I]),
+    "read_su3_soa_ildg_binary": (_I, [_P, C.c_char_p, C.POINTER(_I)]),
     # single-precision twins (sp_*.c) and float <-> double conversions
     "acc_Deo_f": (None, [_P, _P, _P, _P]),
     "acc_Doe_f": (None, [_P, _P, _P, _P]),

@@ -293,6 +293,11 @@ class Reference:
         "ref_md_deltas": (None, [_D, _I, _I, _D, _P]),
         "ref_2mn_gauge": (None, [_P, _P, _D, _I, _I, _D, _I]),
         "ref_rhmc_md": (None, [_P, _P, _P, _D, _I, _I, _P, _P, _P, _D, _I, _D, _I, _I, _D, _I, _D]),
+        "ref_write_ascii": (_I, [_P, C.c_char_p, _I, _P]),
+        "ref_read_ascii": (_I, [_P, C.c_char_p]),
+        "ref_write_ildg": (_I, [_P, C.c_char_p, _I, C.c_char_p]),
+        "ref_read_ildg": (_I, [_P, C.c_char_p]),
+        "ref_set_beta": (None, [_D]),
     }
 
     def __init__(self, dims):
@@ -494,3 +499,21 @@ class Reference:
         self.L.ref_rhmc_md(_p(uo), _p(mo), _p(np.ascontiguousarray(ph)), mass, len(chis), len(a), _p(a), _p(b),
                            _p(chis), res, max_cg, beta, no_md, gauge_scale, t, steps, rho)
         return uo, mo
+
+    # --- configuration files (the reference's io.c) ---
+    def write_ascii(self, u, path, traj, beta=0.0, phases=None):
+        self.L.ref_set_beta(beta)
+        return self.L.ref_write_ascii(_p(u), str(path).encode(), traj, None if phases is None else _p(phases))
+
+    def read_ascii(self, path):
+        u = self.su3()
+        t = self.L.ref_read_ascii(_p(u), str(path).encode())
+        return t, u
+
+    def write_ildg(self, u, path, traj, text=""):
+        return self.L.ref_write_ildg(_p(u), str(path).encode(), traj, text.encode())
+
+    def read_ildg(self, path):
+        u = self.su3()
+        t = self.L.ref_read_ildg(_p(u), str(path).encode())
+        return t, u

@@ -51,6 +51,8 @@
 #include "./md_parameters.h"
 #include "./md_integrator.h"
 #include "./alloc_settings.h"
+#include "./io.h"
+#include "../Include/setting_file_parser.h"
 #include "./sp_struct_c_def.h"
 #include "./sp_alloc_vars.h"
 
@@ -69,6 +71,8 @@ md_param md_parameters;
 int md_dbg_print_count, md_diag_count_fermion, ipdot_f_reset, nMdInversionPerformed;
 
 tamat_soa *ipdot_g_old;
+char input_file_str[MAXLINES * MAXLINELENGTH];
+ferm_param *fermions_parameters;
 int ipdot_g_reset, md_diag_count_gauge;
 /* the benchmark drivers' timing container (test_and_benchmarks.h:31-44) */
 typedef struct { double t[16]; int count; } harness_md_times;
@@ -522,3 +526,17 @@ void ref_rhmc_md(double *u, double *mom, double *ph, double mass, int nps, int o
   aux_th = NULL; aux_ta = NULL;
   stout_globals(0);
 }
+
+/* ---- configuration files (io.c:35-700), host arrays su3_soa[8] ---- */
+int ref_write_ascii(const double *u, const char *path, int traj, const double *phases)
+{
+  return print_su3_soa_ASCII((global_su3_soa *)u, path, traj, (double_soa *)phases);
+}
+int ref_read_ascii(double *u, const char *path) { int t; int rc = read_su3_soa_ASCII((global_su3_soa *)u, path, &t); return rc ? -rc : t; }
+int ref_write_ildg(const double *u, const char *path, int traj, const char *input_text)
+{
+  strncpy(input_file_str, input_text, sizeof(input_file_str) - 1);
+  return print_su3_soa_ildg_binary((global_su3_soa *)u, path, traj);
+}
+int ref_read_ildg(double *u, const char *path) { int t; int rc = read_su3_soa_ildg_binary((global_su3_soa *)u, path, &t); return rc ? -rc : t; }
+void ref_set_beta(double beta) { act_params.beta = beta; }

@@ -41,6 +41,8 @@
 #include "md_parameters.h"
 #include "md_integrator.h"
 #include "random_assignement.h"
+#include "io.h"
+#include "../Include/setting_file_parser.h"
 #define OSTAPLE_HAVE_REFERENCE_TYPES
 #endif
 #include "ostaple_gb300.h"

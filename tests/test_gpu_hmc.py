@@ -159,18 +159,22 @@ def test_fp32_molecular_dynamics_follows_fp64(lat_factory):
 
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])
 def test_thermalisation_from_a_cold_start(lat_factory, precision):
-    """Twelve Metropolis trajectories at beta = 3.75 from unit links: the
-    plaquette falls from 1 and the acceptance stays high; the action the
-    library reports equals the one computed from the plaquette and rectangle
-    sums."""
+    """From unit links at beta = 3.75: six trajectories without the Metropolis
+    test (from the identity the test fails for the first trajectories; the
+    reference's ThermNtraj trajectories skip it, update_versatile.c:581),
+    then eight with it.  The plaquette falls from 1, the Metropolis phase
+    accepts most trajectories, and the action the library reports equals the
+    one from the plaquette and rectangle sums."""
     dims = (8, 8, 8, 8)
     lat = lat_factory(dims)
     u = F.cold_links(dims)
     lat.present(u)
-    out = api.pure_gauge_hmc(u, 3.75, 12, no_md=8, gauge_scale=2, seed=7, precision=precision)
-    assert out["accepted"] >= 9, out
+    therm = api.pure_gauge_hmc(u, 3.75, 6, no_md=8, gauge_scale=2, seed=7, precision=precision, metropolis=False)
+    assert therm["accepted"] == 6
+    assert therm["plaquette"][-1] < 0.9, therm["plaquette"]
+    out = api.pure_gauge_hmc(u, 3.75, 8, no_md=8, gauge_scale=2, seed=7, first_traj=6, precision=precision)
+    assert out["accepted"] >= 6, out
     assert 0.4 < out["plaquette"][-1] < 0.9, out["plaquette"]
-    assert out["plaquette"][-1] < out["plaquette"][0]
     act = api.gauge_action(u, 3.75)
     pl = api.calc_plaquette_soloopenacc(u)
     assert abs(act["plaq_sum"] - pl) <= 1e-12 * abs(pl)
