@@ -3,9 +3,15 @@
 
 Workload: solve (M^+M) x = b with M^+M = m^2 - D_eo D_oe on a 32^4 lattice,
 m = 0.01, to an FP64 true residual sqrt(|b - M^+M x|^2/|b|^2) <= 1e-10 -- the
-configuration the headline metric is quoted on.  Links are seeded
-U = exp(i*0.3*H) (H Gaussian traceless Hermitian per link), staggered phases
-with antiperiodic time boundary, a Gaussian source on the even sites.
+configuration the headline metric is quoted on.  Links: a thermalised
+configuration of the tree-level Symanzik gauge action at beta = 3.75, made
+before the timed region by the library's pure-gauge HMC from a cold start
+(200 trajectories of the reference's integrator, 18 steps x 4 gauge
+substeps, FP32 molecular dynamics, the first 20 without the Metropolis test
+as the reference's thermalisation trajectories), then smeared by 2 stout
+steps of rho = 0.15; staggered phases with antiperiodic time boundary; a
+Gaussian source on the even sites.  --links-source synthetic uses seeded
+U = exp(i*0.3*H) links instead (H Gaussian traceless Hermitian per link).
 
 A step is one complete solve.  `value` is solves per second over all GPUs
 (independent replicas, one per rank, weak scaling), timed with CUDA events on
@@ -125,6 +131,13 @@ def parse_args():
                     help="skip the 4-source x 19-shift multi-shift measurement reported beside the headline")
     ap.add_argument("--delta", type=float, default=1e-4,
                     help="reliable update when |r|^2 < delta * max|r|^2 since the last one")
+    ap.add_argument("--links-source", choices=("thermalized", "synthetic"), default="thermalized",
+                    help="thermalized: pure-gauge HMC configuration + stout smearing; synthetic: exp(i eps H) links")
+    ap.add_argument("--beta", type=float, default=3.75)
+    ap.add_argument("--therm", type=int, default=200, help="pure-gauge HMC trajectories from the cold start")
+    ap.add_argument("--therm-nometro", type=int, default=20,
+                    help="of which the first ones skip the Metropolis test (the reference's ThermNtraj)")
+    ap.add_argument("--stout", type=int, default=2, help="stout steps of rho = 0.15 on the thermalised links")
     return ap.parse_args()
 
 
@@ -205,6 +218,50 @@ def make_inputs(dims, seed, eps):
     return u, ph, b
 
 
+def thermalized_links(lat, dims, seed, args):
+    """A thermalised configuration (outside every timed region): cold start,
+    args.therm pure-gauge tree-level Symanzik HMC trajectories at args.beta
+    with the reference's integrator (18 steps x 4 gauge substeps, length 1),
+    FP32 molecular dynamics, the first args.therm_nometro without the
+    Metropolis test; then args.stout stout steps of rho = 0.15.  Returns the
+    smeared links (host su3_soa[8]) and a summary."""
+    from openstaple_gb300 import api, fields as F
+    from openstaple_gb300.native import act_params
+    u = F.cold_links(dims)
+    lat.present(u)
+    t0 = time.perf_counter()
+    n0 = min(args.therm_nometro, args.therm)
+    a = api.pure_gauge_hmc(u, args.beta, n0, 18, 4, 1.0, seed=seed, first_traj=0, precision="fp32",
+                           metropolis=False)
+    b = api.pure_gauge_hmc(u, args.beta, args.therm - n0, 18, 4, 1.0, seed=seed, first_traj=n0, precision="fp32",
+                           metropolis=True)
+    lat.sync()
+    t_hmc = time.perf_counter() - t0
+    plaq = np.concatenate([a["plaquette"], b["plaquette"]])
+    ds = b["delta_s"]
+    info = {"beta": args.beta, "trajectories": args.therm, "without_metropolis": n0,
+            "accepted_with_metropolis": int(b["accepted"]), "seconds": round(t_hmc, 2),
+            "plaquette_last": float(plaq[-1]) if len(plaq) else None,
+            "plaquette_mean_last_50": float(plaq[-50:].mean()) if len(plaq) else None,
+            "abs_delta_s_mean": float(np.abs(ds).mean()) if len(ds) else None,
+            "integrator": "2MN, 18 steps x 4 gauge substeps, length 1, FP32 molecular dynamics, FP64 Metropolis",
+            "stout": {"steps": args.stout, "rho": 0.15}}
+    if args.stout > 0:
+        api.set_stout_rho(0.15)
+        act_params().stout_steps = args.stout
+        levels = api.su3_field(lat.sizeh, 8 * args.stout)
+        lat.present(levels, copy=False)
+        api.stout_wrapper(u, levels, 0)
+        lat.update_host(levels)
+        out = levels[8 * (args.stout - 1):].copy()
+        lat.release(levels)
+    else:
+        lat.update_host(u)
+        out = u.copy()
+    lat.release(u)
+    return np.ascontiguousarray(out), info
+
+
 def cpu_cg_rate(dims, u, ph, b, mass, res, fp64_iters, budget_s=20.0):
     """Times the oracle port of the reference's FP64 CG (all host threads) on a
     bounded number of iterations and extrapolates to the full solve with the
@@ -233,6 +290,20 @@ def run_reference(args):
     from oracle import Oracle
     threads = os.cpu_count() or 1
     u, ph, b = make_inputs(dims, args.seed, args.eps)
+    therm = None
+    if args.links_source == "thermalized":
+        # the same input configuration as the GPU arm, made by the library's
+        # link generator on the GPU (input data, outside the timed region);
+        # without a GPU the seeded synthetic links stand in, and the line says so
+        import torch
+        if torch.cuda.is_available():
+            from openstaple_gb300 import api
+            torch.cuda.set_device(0)
+            lat = api.Lattice(dims)
+            u, therm = thermalized_links(lat, dims, args.seed, args)
+            lat.close()
+        else:
+            args.links_source = "synthetic (no GPU here to generate the thermalised configuration)"
     o = Oracle(dims, threads=threads)
     times, iters = [], None
     for k in range(args.warmup + args.steps):
@@ -254,7 +325,7 @@ def run_reference(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": f"MdagM CG solve {'x'.join(map(str, dims))} m={args.mass} res={args.res}",
                        "solver": "FP64 CG (inverter_full.c:19-132), oracle port, all host threads",
-                       "cg_iterations": iters},
+                       "cg_iterations": iters, "links": args.links_source, "thermalization": therm},
             "cpu_baseline": {"value": val, "unit": "solves/s", "cores": threads, "kind": "port",
                              "sample": f"{len(times)} full FP64 CG solves"},
             "e2e": {"value": val, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -281,6 +352,9 @@ def main():
     dims = tuple(int(x) for x in args.dims.split(","))
     u, ph, b = make_inputs(dims, args.seed + 17 * rank, args.eps)
     lat = api.Lattice(dims)
+    therm = None
+    if args.links_source == "thermalized":
+        u, therm = thermalized_links(lat, dims, args.seed + 17 * rank, args)
     api.set_sloppy_links(args.links)
     bytes_deo, bytes_doe = (BYTES_Q16_DEO, BYTES_Q16_SIGN) if args.links == "q16" else (BYTES_F32_DEO, BYTES_F32_SIGN)
     stream = torch.cuda.Stream()
@@ -480,7 +554,10 @@ def main():
             "metric": "MdagM solves/s to FP64 true residual 1e-10", "value": value, "unit": "solves/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
-            "data": "synthetic (seeded exp(i*0.3*H) links, Gaussian source)",
+            "data": ("synthetic: thermalised tree-level Symanzik configuration at beta=%g (library pure-gauge HMC "
+                     "from a cold start, %d trajectories) + %d stout steps rho=0.15, Gaussian source"
+                     % (args.beta, args.therm, args.stout) if args.links_source == "thermalized" else
+                     "synthetic (seeded exp(i*0.3*H) links, Gaussian source)"),
             "config": {"workload": f"MdagM solve {'x'.join(map(str, dims))} m={args.mass} to FP64 true residual "
                                    f"{args.res}",
                        "solver": ("flexible CG preconditioned by the learned gauge-covariant network (tcgen05 BF16), "
@@ -493,12 +570,17 @@ def main():
                        "rhs_per_step": nrhs,
                        "batched_4rhs": batched4,
                        "multishift_4x19": multishift,
+                       "links": args.links_source,
+                       "thermalization": therm,
                        "reliable_every": args.every,
                        "iterations": infos[-1]["iters"], "reliable_updates": infos[-1]["n_reliable"],
                        "true_residual": infos[-1]["true_res"], "all_converged": ok,
                        "plain_fp64_cg": {"ms": fp64["ms"], "iterations": fp64["iters"], "status": fp64["status"]},
                        "speedup_vs_plain_fp64_cg": fp64["ms"] * nrhs / ms if fp64["ms"] else None,
-                       "l2": "inputs larger than L2 (FP32 links 201 MB, FP64 links 604 MB > 129 MB)",
+                       "l2": ("inputs larger than L2: the FP32 iteration streams %.0f MB of 16-bit links, %.0f MB "
+                              "of FP32 vectors and reads the FP64 links (%.0f MB) at reliable updates; L2 is "
+                              "126 MB" % (8 * 24 * lat.sizeh / 1e6, 5 * 24 * lat.sizeh / 1e6,
+                                          8 * 9 * 16 * lat.sizeh / 1e6)),
                        "parallelism": f"replicas x{world}"},
             "roofline": {"kernel": "k_mx_deo_dot (FP32 D_eo + M^+M epilogue + <p,Ap>, "
                                    + ("16-bit fixed-point links" if args.links == "q16" else "FP32 two-row links")

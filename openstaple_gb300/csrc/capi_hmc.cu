@@ -301,7 +301,7 @@ int ostaple_pure_gauge_hmc(su3_soa* u, double beta, int ntraj, int no_md, int ga
       for (int c = 0; c < 2 * no_md; ++c) gauge_2mn_fused<double>(U, mom, dl, gauge_scale);
     } else {
       launch_links_64_to_32(U.p, 9, u32, st);
-      HmcLinks<float> U32{u32, 6};
+      HmcLinks<float> U32{u32, 0};   // array-of-structures FP32 copy
       for (int c = 0; c < 2 * no_md; ++c) gauge_2mn_fused<float>(U32, mom32, dl, gauge_scale);
       launch_links_32_to_64(u32, U.p, 9, st);
       launch_alg_32_to_64(mom32, mom, st);

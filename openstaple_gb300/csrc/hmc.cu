@@ -37,14 +37,36 @@ template <typename C> OST_D void rebuild2(Mt<C>& a) {
   a.m[2][2] = conj_cross(a.m[0][0], a.m[1][1], a.m[0][1], a.m[1][0]);
 }
 
-// U_mu(y), rows 0-1 loaded, row 2 rebuilt
+// U_mu(y), rows 0-1 loaded, row 2 rebuilt.  rows = 9 or 6: structure of
+// arrays (rows complex arrays per direction); rows = 0: the link generator's
+// array of structures, the 6 complex numbers of a link contiguous (48 bytes
+// in FP32: three 16-byte loads)
+template <typename C> OST_D void ld_rows(const C* u, int rows, long sh, int dir, long i, C m[6]) {
+  if (rows == 0) {
+    const C* b = u + (long(dir) * sh + i) * 6;
+    if constexpr (sizeof(C) == 8) {
+      const float4* q = reinterpret_cast<const float4*>(b);
+      const float4 a0 = __ldg(q), a1 = __ldg(q + 1), a2 = __ldg(q + 2);
+      m[0] = cmk<C>(a0.x, a0.y); m[1] = cmk<C>(a0.z, a0.w); m[2] = cmk<C>(a1.x, a1.y);
+      m[3] = cmk<C>(a1.z, a1.w); m[4] = cmk<C>(a2.x, a2.y); m[5] = cmk<C>(a2.z, a2.w);
+    } else {
+#pragma unroll
+      for (int k = 0; k < 6; ++k) m[k] = __ldg(b + k);
+    }
+    return;
+  }
+  const C* b = u + long(dir) * rows * sh + i;
+#pragma unroll
+  for (int k = 0; k < 6; ++k) m[k] = __ldg(b + k * sh);
+}
 template <typename C> OST_D Mt<C> ld_u(const C* u, int rows, long sh, int dir, long i) {
   Mt<C> a;
-  const C* b = u + long(dir) * rows * sh + i;
+  C m[6];
+  ld_rows(u, rows, sh, dir, i, m);
 #pragma unroll
   for (int r = 0; r < 2; ++r)
 #pragma unroll
-    for (int c = 0; c < 3; ++c) a.m[r][c] = __ldg(b + (r * 3 + c) * sh);
+    for (int c = 0; c < 3; ++c) a.m[r][c] = m[r * 3 + c];
   rebuild2(a);
   return a;
 }
@@ -123,23 +145,27 @@ template <typename C> struct Walker {
   int rows;
   Pos x;
   int px;   // parity of x
-  // U_mu(x + a e_s + b e_t)
+  // U_mu(x + a e_s + b e_t), |a|, |b| <= 2; every coordinate shifted and
+  // wrapped with selects (no indexed local array)
   OST_D Mt<C> at(int mu, int s, int a, int t, int b) const {
-    const int n[4] = {g.n0, g.n1, g.n2, g.n3};
-    int d[4] = {x.d[0], x.d[1], x.d[2], x.d[3]};
-    d[s] = wrap(d[s] + a, n[s]);
-    d[t] = wrap(d[t] + b, n[t]);
-    const long lex = d[0] + long(d[1]) * g.vol1 + long(d[2]) * g.vol2 + long(d[3]) * g.vol3;
+    const int e0 = wrap(x.d[0] + (s == 0 ? a : 0) + (t == 0 ? b : 0), g.n0);
+    const int e1 = wrap(x.d[1] + (s == 1 ? a : 0) + (t == 1 ? b : 0), g.n1);
+    const int e2 = wrap(x.d[2] + (s == 2 ? a : 0) + (t == 2 ? b : 0), g.n2);
+    const int e3 = wrap(x.d[3] + (s == 3 ? a : 0) + (t == 3 ? b : 0), g.n3);
+    const long lex = e0 + long(e1) * g.vol1 + long(e2) * g.vol2 + long(e3) * g.vol3;
     const int p = px ^ ((a + b) & 1);
     return ld_u(u, rows, long(g.sizeh), 2 * mu + p, lex >> 1);
   }
 };
 
-// the staple parts of link (x, m), C_ZERO / C_ONE included
-template <typename C>
-OST_D Mt<C> gauge_staple(const Walker<C>& w, int m, int parts) {
+// the staple parts of link (x, M), C_ZERO / C_ONE included.  M is a
+// template parameter and the loop over nu is unrolled, so every neighbour
+// offset is a compile-time constant.
+template <typename C, int M>
+OST_D Mt<C> gauge_staple_t(const Walker<C>& w, int parts) {
   typedef decltype(C().x) Rt;
   const Rt c0 = Rt(HMC_C_ZERO), c1 = Rt(HMC_C_ONE);
+  constexpr int m = M;
   Mt<C> S = mzero_t<C>();
 #pragma unroll 1
   for (int n = 0; n < 4; ++n) {
@@ -169,6 +195,16 @@ OST_D Mt<C> gauge_staple(const Walker<C>& w, int m, int parts) {
     }
   }
   return S;
+}
+
+template <typename C>
+OST_D Mt<C> gauge_staple(const Walker<C>& w, int m, int parts) {
+  switch (m) {
+    case 0: return gauge_staple_t<C, 0>(w, parts);
+    case 1: return gauge_staple_t<C, 1>(w, parts);
+    case 2: return gauge_staple_t<C, 2>(w, parts);
+    default: return gauge_staple_t<C, 3>(w, parts);
+  }
 }
 
 // tamat / thmat access in precision R (per direction: 3 complex arrays, then 2 real)
@@ -434,11 +470,16 @@ k_mom_exp(long sh, C* u, int rows, const decltype(C().x)* __restrict__ mom, doub
 #pragma unroll
   for (int c = 0; c < 3; ++c) n1 += r.m[1][c].x * r.m[1][c].x + r.m[1][c].y * r.m[1][c].y;
   n1 = Rt(1) / sqrt(n1);
-  C* base = u + long(dir) * rows * sh + x;
 #pragma unroll
-  for (int c = 0; c < 3; ++c) {
-    base[c * sh] = r.m[0][c];
-    base[(3 + c) * sh] = cscale(r.m[1][c], n1);
+  for (int c = 0; c < 3; ++c) r.m[1][c] = cscale(r.m[1][c], n1);
+  if (rows == 0) {
+    C* base = u + (long(dir) * sh + x) * 6;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) { base[c] = r.m[0][c]; base[3 + c] = r.m[1][c]; }
+  } else {
+    C* base = u + long(dir) * rows * sh + x;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) { base[c * sh] = r.m[0][c]; base[(3 + c) * sh] = r.m[1][c]; }
   }
 }
 
@@ -611,10 +652,11 @@ __global__ void k_links_64_to_32(const double2* __restrict__ u64, int rows64, fl
   if (t >= 8L * sh) return;
   const int dir = int(t / sh);
   const long x = t - long(dir) * sh;
+  float2* o = u32 + (long(dir) * sh + x) * 6;   // array of structures: a link's 6 numbers contiguous
 #pragma unroll
   for (int k = 0; k < 6; ++k) {
     const double2 v = u64[(long(dir) * rows64 + k) * sh + x];
-    u32[(long(dir) * 6 + k) * sh + x] = make_float2(float(v.x), float(v.y));
+    o[k] = make_float2(float(v.x), float(v.y));
   }
 }
 
@@ -629,7 +671,7 @@ __global__ void k_links_32_to_64(const float2* __restrict__ u32, double2* u64, i
   for (int r = 0; r < 2; ++r)
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-      const float2 v = u32[(long(dir) * 6 + r * 3 + c) * sh + x];
+      const float2 v = u32[(long(dir) * sh + x) * 6 + r * 3 + c];
       a.m[r][c] = make_double2(v.x, v.y);
     }
   double n0 = 0;

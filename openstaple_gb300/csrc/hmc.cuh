@@ -4,8 +4,10 @@
 // of the link generator).
 //
 // Link views: `rows` complex arrays per direction, the first two rows of
-// every link stored (rows = 9: the reference su3_soa layout; rows = 6: the
-// library's compact two-row copy).  Momenta and forces are thmat_soa[8] /
+// every link stored (rows = 9: the reference su3_soa layout; rows = 6: a
+// compact two-row copy), or rows = 0: an array of structures with the six
+// complex numbers of rows 0-1 of each link contiguous (the link generator's
+// FP32 copy).  Momenta and forces are thmat_soa[8] /
 // tamat_soa[8] in the reference layout (per direction 3 complex then 2 real
 // arrays of sizeh) in the kernel's precision.
 #pragma once
@@ -55,8 +57,8 @@ void launch_gen_momenta(R* mom, unsigned long long seed, unsigned long long stre
 // Gaussian vec3_soa (3*sizeh complex numbers, real and imaginary parts of
 // variance 1/2) from the same generator
 void launch_gen_vec3_gauss(double2* v, unsigned long long seed, unsigned long long stream, cudaStream_t st);
-// FP64 reference-layout links <-> compact two-row FP32 links; the way back
-// reunitarises rows 0-1 in FP64
+// FP64 reference-layout links <-> the FP32 array-of-structures copy (rows
+// 0-1 of a link contiguous); the way back reunitarises rows 0-1 in FP64
 void launch_links_64_to_32(const double2* u64, int rows64, float2* u32, cudaStream_t st);
 void launch_links_32_to_64(const float2* u32, double2* u64, int rows64, cudaStream_t st);
 void launch_alg_64_to_32(const double* a64, float* a32, cudaStream_t st);

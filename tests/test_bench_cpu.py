@@ -49,7 +49,7 @@ def _json_lines(text):
 
 def test_reference_arm_prints_one_line(built):
     r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference", "--dims", "4,4,4,4",
-                        "--steps", "1", "--warmup", "1"], capture_output=True, text=True, timeout=300, cwd=ROOT)
+                        "--steps", "1", "--warmup", "1", "--links-source", "synthetic"], capture_output=True, text=True, timeout=300, cwd=ROOT)
     assert r.returncode == 0, r.stderr
     lines = _json_lines(r.stdout)
     assert len(lines) == 1
@@ -64,7 +64,8 @@ def test_reference_arm_under_torchrun_only_rank0_prints(built):
     port = _free_port()
     r = subprocess.run([sys.executable, "-m", "torch.distributed.run", "--nnodes", "1", "--nproc-per-node", "2",
                         "--master-addr", "127.0.0.1", "--master-port", str(port), str(ROOT / "bench.py"),
-                        "--impl", "reference", "--gpus", "2", "--dims", "4,4,4,4", "--steps", "1", "--warmup", "0"],
+                        "--impl", "reference", "--gpus", "2", "--dims", "4,4,4,4", "--steps", "1", "--warmup", "0",
+                        "--links-source", "synthetic"],
                        capture_output=True, text=True, timeout=300, cwd=ROOT)
     assert r.returncode == 0, r.stderr[-2000:]
     lines = _json_lines(r.stdout)
