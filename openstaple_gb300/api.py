@@ -44,6 +44,10 @@ class Lattice:
         if not arr.flags["C_CONTIGUOUS"]:
             raise ValueError("arrays must be C-contiguous")
         p = arr.ctypes.data
+        if p in self._present and self._present[p] != arr.nbytes:
+            # the mapping of a freed array that lay at the same host address
+            self.L.ostaple_exit_data(p)
+            del self._present[p]
         if p not in self._present:
             check(self.L.ostaple_enter_data(p, arr.nbytes), "enter_data")
             self._present[p] = arr.nbytes

@@ -335,7 +335,11 @@ def test_force_with_batched_pseudofermions_equals_sequential(lat_factory, accel,
                                         taux.ctypes.data, shiftmulti.ctypes.data, ip, 10000)
         api.check(0, "fermion_force_soloopenacc")
         lat.update_host(shiftmulti)
-        return lat.update_host(ipdot), shiftmulti.copy(), lat.update_host(s).copy()
+        out = lat.update_host(ipdot).copy(), shiftmulti.copy(), lat.update_host(s).copy()
+        # the per-call arrays are freed on return: drop their device mirrors
+        for arr in (stout_levels, gl3, ipdot, taux, shiftmulti, shifttemp, r, h, s, p):
+            lat.release(arr)
+        return out
 
     t = api.inverter_tricks()
     t.singlePInvAccelMultiInv, t.useMixedPrecision = 0, 0
