@@ -191,17 +191,6 @@ unsigned long long ostaple_kernel_launches(void);
  * full host-link bandwidth (cudaHostRegister).  No reference counterpart. */
 int ostaple_pin_host(void *host, size_t bytes);
 int ostaple_unpin_host(void *host);
-/* Mean milliseconds of one launch of a hot kernel, timed with CUDA events on
- * its own stream: which = 0 FP64 D_eo (as acc_Deo), 1 FP32 D_oe of the mixed
- * solver, 2 FP32 fused D_eo + M^+M epilogue + <p,Ap>.  No reference
- * counterpart (measurement hook). */
-int ostaple_time_kernel(int which, const su3_soa *u, const double_soa *phases, int reps, double *ms);
-
-/* Measured FMA throughput of this device in TFLOP/s (fp64 != 0: FP64, else
- * FP32); the ceiling of the compute-bound FP64 kernels.  No reference
- * counterpart. */
-int ostaple_probe_fma_tflops(int fp64, double *tflops);
-
 /* Launch-shape autotuner of the FP32 D_oe hops (the mixed solver's block
  * size, the batched and multi-shift solvers' systems per thread).  Only
  * shapes that leave every result bit unchanged are tuned; each (kernel,

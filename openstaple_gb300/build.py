@@ -3,6 +3,8 @@
 * ``openstaple_gb300/libostaple_gb300.so`` -- the CUDA hot path for sm_103a,
   compiled with nvcc (one translation unit per kernel family, compiled in
   parallel, linked as a plain shared library with a C ABI).
+* ``openstaple_gb300/libostaple_gb300_bench.so`` -- the benchmark's
+  measurement entry points (``csrc/bench/``), linked against the library.
 * ``oracle/liboracle.so`` -- the CPU restatement used by the tests as the
   parity checker (plain C, gcc, OpenMP).
 * ``oracle/_ref/libref_<dims>.so`` -- the reference's own C sources compiled
@@ -24,6 +26,7 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 BUILD = ROOT / "_build"
 LIB = PKG / "libostaple_gb300.so"
+BENCH_LIB = PKG / "libostaple_gb300_bench.so"
 ORACLE_DIR = ROOT / "oracle"
 ORACLE_LIB = ORACLE_DIR / "liboracle.so"
 REF_OUT = ORACLE_DIR / "_ref"
@@ -81,6 +84,16 @@ def build_library(verbose: bool = False) -> Path:
     return LIB
 
 
+def build_bench_library(verbose: bool = False) -> Path:
+    nvcc = _nvcc()
+    srcs = sorted((CSRC / "bench").glob("*.cu"))
+    headers = list(CSRC.glob("*.cuh")) + list((ROOT / "include").glob("*.h"))
+    if _newer([*srcs, *headers, LIB], BENCH_LIB):
+        _run([nvcc, *ARCH, *NVCC_FLAGS, "-shared", "-o", str(BENCH_LIB), *map(str, srcs),
+              "-L", str(PKG), "-lostaple_gb300", "-Xlinker", "-rpath,$ORIGIN", "-lcudart"])
+    return BENCH_LIB
+
+
 def build_oracle(verbose: bool = False) -> Path:
     srcs = sorted(ORACLE_DIR.glob("*.c"))
     srcs = [s for s in srcs if s.name != "ref_harness.c"]
@@ -117,6 +130,7 @@ def build_all(verbose: bool = False) -> None:
                 ex.submit(build_reference_oracles, REF_DIMS, verbose)]
         for f in futs:
             f.result()
+    build_bench_library(verbose)
 
 
 if __name__ == "__main__":

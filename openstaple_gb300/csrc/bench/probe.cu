@@ -1,9 +1,16 @@
-// probe.cu -- measures the device's FP64 and FP32 FMA throughput, the
-// roofline ceiling of the compute-bound FP64 kernels (the driver-measured
-// peaks cover only HBM bandwidth and BF16 tensor throughput).
+// probe.cu -- the benchmark library (libostaple_gb300_bench.so, not part of
+// the drop-in): the device's FP64 and FP32 FMA throughput, the roofline
+// ceiling of the compute-bound FP64 kernels (the measured peaks of the
+// machine cover HBM bandwidth and BF16 tensor throughput only), and the
+// per-launch timing of the hot kernels that the benchmark's roofline uses.
 #include <cstdio>
-#include "runtime.cuh"
-#include "../../include/ostaple_gb300.h"
+#include "../runtime.cuh"
+#include "../../../include/ostaple_gb300.h"
+#include "../../../include/ostaple_gb300_bench.h"
+
+namespace ost {
+int time_hot_kernel(int which, const su3_soa* u, const double_soa* phases, int reps, double* ms);
+}
 
 namespace {
 
@@ -53,4 +60,8 @@ extern "C" int ostaple_probe_fma_tflops(int fp64, double* tflops) {
   if (!ost::require_init("ostaple_probe_fma_tflops")) return -2;
   *tflops = fp64 ? run<double>(256) : run<float>(8192);
   return ost::error_code();
+}
+
+extern "C" int ostaple_time_kernel(int which, const su3_soa* u, const double_soa* phases, int reps, double* ms) {
+  return ost::time_hot_kernel(which, u, phases, reps, ms);
 }

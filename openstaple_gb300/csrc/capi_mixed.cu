@@ -256,12 +256,61 @@ int ostaple_invert_mixed(const su3_soa* u, const double_soa* phases, double mass
   return r.converged ? INVERTER_SUCCESS : INVERTER_FAILURE;
 }
 
+int ostaple_mdagm_df(const su3_soa* u, const double_soa* phases, double mass, double shift, vec3_soa* out,
+                     const vec3_soa* in) {
+  if (!require_init("ostaple_mdagm_df")) return -2;
+  cudaStream_t st = rt().stream;
+  const Z* u64 = dev(reinterpret_cast<const Z*>(u), "u");
+  const void* ph = resolve(phases, "phases");
+  const Z* din = dev(reinterpret_cast<const Z*>(in), "in");
+  Z* dout = dev(reinterpret_cast<Z*>(out), "out");
+  if (!u64 || !ph || !din || !dout) return -3;
+  PreparedF32 pf;
+  if (!prepare_f32(u64, nullptr, static_cast<const double*>(ph), &pf, st)) return -4;
+  DfOperator op;
+  DfWork w;
+  if (!prepare_df(u64, pf, &op, &w, st)) {
+    set_error(-12, "ostaple_mdagm_df: phases must be 0 or pi (staggered phases and boundary signs)");
+    return -12;
+  }
+  df_mdagm(op, w, dout, din, mass * mass + shift, st);
+  OST_CUDA(cudaStreamSynchronize(st));
+  return error_code();
+}
+
+// Exits on a failure in a critical region, as the reference does
+// (inverter_wrappers.c:24-39).
+void convergence_messages(int conv_importance, int inverter_status) {
+  if (inverter_status == INVERTER_FAILURE) {
+    if (conv_importance == CONVERGENCE_CRITICAL) {
+      printf("\n\n\t\tERROR : inverter failed to converge in a critical region of the code. Exiting now!!\n\n");
+      exit(1);
+    }
+    printf("\n\t\tWARNING : inverter failed to converge.\n");
+  }
+}
+
+int inverter_wrapper(inverter_package ip, ferm_param* pars, vec3_soa* out, const vec3_soa* in, double res,
+                     int max_cg, double shift, int convergence_importance) {
+  int cg = 0, st;
+  if (inverter_tricks.useMixedPrecision)
+    st = inverter_mixed_precision(ip, pars, out, in, res, max_cg, shift, &cg);
+  else
+    st = ker_invert_openacc(ip.u, pars, out, in, res, ip.loc_r, ip.loc_h, ip.loc_s, ip.loc_p, max_cg, shift, &cg);
+  convergence_messages(convergence_importance, st);
+  return cg;
+}
+
+}  // extern "C"
+
+namespace ost {
+
 // Mean duration (ms) of one launch of a hot kernel, timed with CUDA events on
 // the stream it is launched on: which = 0: FP64 D_eo (reference layout and
 // angle phases, as acc_Deo); 1: FP32 D_oe of the mixed solver; 2: FP32 fused
-// D_eo + M^+M epilogue + <p, Ap> of the mixed solver.  Measurement hook for
-// the benchmark; no reference counterpart.
-int ostaple_time_kernel(int which, const su3_soa* u, const double_soa* phases, int reps, double* ms) {
+// D_eo + M^+M epilogue + <p, Ap> of the mixed solver; 3: double-float M^+M.
+// Internal: the benchmark library's ostaple_time_kernel calls it.
+int time_hot_kernel(int which, const su3_soa* u, const double_soa* phases, int reps, double* ms) {
   if (!require_init("ostaple_time_kernel")) return -2;
   cudaStream_t st = rt().stream;
   const Z* u64 = dev(reinterpret_cast<const Z*>(u), "u");
@@ -333,49 +382,4 @@ int ostaple_time_kernel(int which, const su3_soa* u, const double_soa* phases, i
   return error_code();
 }
 
-int ostaple_mdagm_df(const su3_soa* u, const double_soa* phases, double mass, double shift, vec3_soa* out,
-                     const vec3_soa* in) {
-  if (!require_init("ostaple_mdagm_df")) return -2;
-  cudaStream_t st = rt().stream;
-  const Z* u64 = dev(reinterpret_cast<const Z*>(u), "u");
-  const void* ph = resolve(phases, "phases");
-  const Z* din = dev(reinterpret_cast<const Z*>(in), "in");
-  Z* dout = dev(reinterpret_cast<Z*>(out), "out");
-  if (!u64 || !ph || !din || !dout) return -3;
-  PreparedF32 pf;
-  if (!prepare_f32(u64, nullptr, static_cast<const double*>(ph), &pf, st)) return -4;
-  DfOperator op;
-  DfWork w;
-  if (!prepare_df(u64, pf, &op, &w, st)) {
-    set_error(-12, "ostaple_mdagm_df: phases must be 0 or pi (staggered phases and boundary signs)");
-    return -12;
-  }
-  df_mdagm(op, w, dout, din, mass * mass + shift, st);
-  OST_CUDA(cudaStreamSynchronize(st));
-  return error_code();
-}
-
-// Exits on a failure in a critical region, as the reference does
-// (inverter_wrappers.c:24-39).
-void convergence_messages(int conv_importance, int inverter_status) {
-  if (inverter_status == INVERTER_FAILURE) {
-    if (conv_importance == CONVERGENCE_CRITICAL) {
-      printf("\n\n\t\tERROR : inverter failed to converge in a critical region of the code. Exiting now!!\n\n");
-      exit(1);
-    }
-    printf("\n\t\tWARNING : inverter failed to converge.\n");
-  }
-}
-
-int inverter_wrapper(inverter_package ip, ferm_param* pars, vec3_soa* out, const vec3_soa* in, double res,
-                     int max_cg, double shift, int convergence_importance) {
-  int cg = 0, st;
-  if (inverter_tricks.useMixedPrecision)
-    st = inverter_mixed_precision(ip, pars, out, in, res, max_cg, shift, &cg);
-  else
-    st = ker_invert_openacc(ip.u, pars, out, in, res, ip.loc_r, ip.loc_h, ip.loc_s, ip.loc_p, max_cg, shift, &cg);
-  convergence_messages(convergence_importance, st);
-  return cg;
-}
-
-}  // extern "C"
+}  // namespace ost

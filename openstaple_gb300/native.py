@@ -10,6 +10,7 @@ import ctypes as C
 from pathlib import Path
 
 LIB_PATH = Path(__file__).resolve().parent / "libostaple_gb300.so"
+BENCH_LIB_PATH = Path(__file__).resolve().parent / "libostaple_gb300_bench.so"
 MAX_APPROX_ORDER = 25  # rationalapprox.h:8
 INVERTER_SUCCESS = 1
 INVERTER_FAILURE = 0
@@ -97,11 +98,9 @@ SIGNATURES = {
     "ostaple_update_device": (_I, [_P, C.c_size_t]),
     "ostaple_update_host": (_I, [_P, C.c_size_t]),
     "ostaple_deviceptr": (_P, [_P]),
-    "ostaple_probe_fma_tflops": (_I, [_I, C.POINTER(_D)]),
     "ostaple_kernel_launches": (C.c_ulonglong, []),
     "ostaple_pin_host": (_I, [_P, C.c_size_t]),
     "ostaple_unpin_host": (_I, [_P]),
-    "ostaple_time_kernel": (_I, [_I, _P, _P, _I, C.POINTER(_D)]),
     "ostaple_autotune": (_I, [_I]),
     "ostaple_autotune_report": (_I, [C.c_char_p, _I]),
     "acc_Deo": (None, [_P, _P, _P, _P]),
@@ -255,6 +254,26 @@ def lib() -> C.CDLL:
         L.initialize_md_global_variables.argtypes = [MdParam]
         _lib = L
     return _lib
+
+
+_bench_lib = None
+
+
+def bench_lib() -> C.CDLL:
+    """Loads the benchmark's measurement library (kernel timing, FMA probe)."""
+    global _bench_lib
+    if _bench_lib is None:
+        lib()
+        if not BENCH_LIB_PATH.exists():
+            raise RuntimeError(f"{BENCH_LIB_PATH} is missing: build it with `python -c 'import __graft_entry__ as g; "
+                               "g.build()'`")
+        L = C.CDLL(str(BENCH_LIB_PATH), mode=C.RTLD_LOCAL)
+        L.ostaple_probe_fma_tflops.restype = C.c_int
+        L.ostaple_probe_fma_tflops.argtypes = [C.c_int, C.POINTER(C.c_double)]
+        L.ostaple_time_kernel.restype = C.c_int
+        L.ostaple_time_kernel.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.POINTER(C.c_double)]
+        _bench_lib = L
+    return _bench_lib
 
 
 class MdParam(C.Structure):

@@ -31,11 +31,21 @@ def test_header_declares_reference_entry_points():
         assert ref_name in names
 
 
+def declared_in(header):
+    return [n for n in declared_functions() if re.search(r"\b%s\s*\(" % n, (ROOT / "include" / header).read_text())]
+
+
 def test_library_exports_every_declared_symbol(built):
-    from openstaple_gb300.native import LIB_PATH
+    from openstaple_gb300.native import BENCH_LIB_PATH, LIB_PATH
     L = ctypes.CDLL(str(LIB_PATH))
-    missing = [n for n in declared_functions() if not hasattr(L, n)]
+    missing = [n for n in declared_in("ostaple_gb300.h") if not hasattr(L, n)]
     assert not missing, f"declared but not exported: {missing}"
+    # the measurement entry points live in the benchmark library only
+    LB = ctypes.CDLL(str(BENCH_LIB_PATH))
+    bench = declared_in("ostaple_gb300_bench.h")
+    assert sorted(bench) == ["ostaple_probe_fma_tflops", "ostaple_time_kernel"]
+    assert all(hasattr(LB, n) for n in bench)
+    assert not any(hasattr(L, n) for n in bench)
     # the weak inverter_tricks global is exported too
     assert ctypes.c_int.in_dll(L, "inverter_tricks") is not None
 
