@@ -402,6 +402,15 @@ void convergence_messages(int conv_importance, int inverter_status);
 int inverter_wrapper(inverter_package ip, ferm_param *pars, vec3_soa *out, const vec3_soa *in, double res,
                      int max_cg, double shift, int convergence_importance);
 
+/* ---- full-D inversion for the fermionic measurements (ferm_meas.h) ------ */
+/* Solves the full staggered matrix D (out_e, out_o) = (in_e, in_o) by
+ * even/odd reduction: phi_e = m in_e - D_eo in_o, out_e = (M^+M)^-1 phi_e
+ * through inverter_wrapper (zero guess, CONVERGENCE_CRITICAL), out_o =
+ * (in_o - D_oe out_e) / m.  phi_e and phi_o are work fields
+ * (Meas/ferm_meas.c:50-71). */
+void eo_inversion(inverter_package ip, ferm_param *tfermions_parameters, double res, int max_cg, vec3_soa *in_e,
+                  vec3_soa *in_o, vec3_soa *out_e, vec3_soa *out_o, vec3_soa *phi_e, vec3_soa *phi_o);
+
 /* ---- stout smearing (stouting.h:13-44) ---------------------------------- */
 /* U' = exp(-Q_A) U with Q_A = rho/C_0 TA(U C), C the tree-level-Symanzik
  * weighted staples; writes uprime (rows 0,1), local_staples (if not NULL)

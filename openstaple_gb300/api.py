@@ -375,6 +375,27 @@ def gauge_action(u, beta: float) -> dict:
 
 
 # ---- batched solvers ----
+def eo_inversion(ip, fp, res: float, max_cg: int, in_e, in_o, out_e, out_o, phi_e, phi_o) -> None:
+    """Full-D inversion by even/odd reduction (Meas/ferm_meas.c:50-71)."""
+    lib().eo_inversion(ip, C.byref(fp), res, max_cg, ptr(in_e), ptr(in_o), ptr(out_e), ptr(out_o), ptr(phi_e),
+                       ptr(phi_o))
+    check(0, "eo_inversion")
+
+
+def chiral_condensate(in_e, in_o, out_e, out_o, degeneracy: int, volume: int) -> complex:
+    """The chiral condensate estimator of one noise vector,
+    degeneracy / 4 / V * (<in_e, out_e> + <in_o, out_o>) with out = D^-1 in
+    (Meas/ferm_meas.c:295, 314-321), from the library's global scalar
+    products (the fields must be present)."""
+    L = lib()
+    a = np.zeros(2)
+    b = np.zeros(2)
+    L.scal_prod_global_ri(ptr(in_e), ptr(out_e), a.ctypes.data_as(C.POINTER(C.c_double)))
+    L.scal_prod_global_ri(ptr(in_o), ptr(out_o), b.ctypes.data_as(C.POINTER(C.c_double)))
+    check(0, "scal_prod_global_ri")
+    return degeneracy * 0.25 / volume * complex(a[0] + b[0], a[1] + b[1])
+
+
 def invert_mixed_batch(u, phases, mass: float, solutions, sources, shifts=None, res: float = 1e-10,
                        max_iter: int = 100000, delta_frac: float = 0.0) -> dict:
     """(M^+M + shift_k) x_k = b_k for all k at once (links read once per Dslash per batch of 8)."""

@@ -10,11 +10,8 @@
 // immediately when the recursion has converged (done) or asks for a reliable
 // update (need_rel), so replaying a chunk past either point does no work.
 #include <cmath>
-#include <cstdlib>
 #include <cstring>
-#include <map>
 #include <type_traits>
-#include <utility>
 #include "autotune.cuh"
 #include "dslash.cuh"
 #include "kernels.cuh"
@@ -103,11 +100,7 @@ void phases_to_f32(const double* ph64, float* ph32, long sh, cudaStream_t st) {
 }
 
 // ---- FP32 iteration kernels ----
-// HB hops' loads in flight per thread.  A thread handles the sites idx,
-// idx + grid, idx + 2 grid, ...: with one block per `threads` sites (the
-// default) that is one site; with OSTAPLE_HOP_GRID=wave the grid is one
-// resident wave (no partially filled last wave) and every thread walks about
-// sizeh / (wave size) sites.
+// One thread per site; HB hops' loads in flight per thread.
 
 // t = D_oe p (any block size up to 256: the autotuner picks the shape)
 template <int PH, typename LV, int HB>
@@ -115,19 +108,17 @@ __global__ void __launch_bounds__(256)
 k_mx_doe(Geom g, LV u, const void* __restrict__ ph, const float2* __restrict__ p, float2* __restrict__ t,
          const MixScal* sc) {
   if (halted(sc)) return;   // set by k_mx_update, two launches back
-  int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  const int stride = gridDim.x * blockDim.x;
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
   // launched early (programmatic dependent launch): fetch the links, which
   // no kernel of the solve writes, while the previous kernel finishes
   if (idx < g.sizeh) prefetch_links<1>(g, u, idx);
   pdl_wait();               // p from k_mx_pupdate
   pdl_trigger();
-  for (; idx < g.sizeh; idx += stride) {
-    float2 aux[3];
-    hop_fb<1, PH, LV, HB>(g, u, p, ph, idx, aux);
+  if (idx >= g.sizeh) return;
+  float2 aux[3];
+  hop_fb<1, PH, LV, HB>(g, u, p, ph, idx, aux);
 #pragma unroll
-    for (int c = 0; c < 3; ++c) t[c * long(g.sizeh) + idx] = make_float2(0.5f * aux[c].x, 0.5f * aux[c].y);
-  }
+  for (int c = 0; c < 3; ++c) t[c * long(g.sizeh) + idx] = make_float2(0.5f * aux[c].x, 0.5f * aux[c].y);
 }
 
 // s = m2 p - D_eo t ; pAp = Re<p, s> ; alpha = delta / pAp
@@ -136,14 +127,13 @@ __global__ void __launch_bounds__(MX_THREADS)
 k_mx_deo_dot(Geom g, LV u, const void* __restrict__ ph, const float2* __restrict__ t, const float2* __restrict__ p,
              float2* __restrict__ s, MixScal* sc, ReduceWs ws) {
   if (halted(sc)) return;
-  int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  const int stride = gridDim.x * blockDim.x;
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
   if (idx < g.sizeh) prefetch_links<0>(g, u, idx);   // as in k_mx_doe
   pdl_wait();               // t from k_mx_doe
   pdl_trigger();
   float v[1] = {0.0f};
-  const float m2 = float(sc->m2);
-  for (; idx < g.sizeh; idx += stride) {
+  if (idx < g.sizeh) {
+    const float m2 = float(sc->m2);
     float2 aux[3];
     hop_fb<0, PH, LV, HB>(g, u, t, ph, idx, aux);
 #pragma unroll
@@ -353,47 +343,15 @@ void with_sloppy_links(const MixedBuffers& B, F&& f) {
   else f(LinkView<float2>{B.u32, rt().g.sizeh, B.u32_compact ? 6 : 9});
 }
 
-bool hop_grid_wave() {
-  static const int wave = [] {
-    const char* e = std::getenv("OSTAPLE_HOP_GRID");
-    return e && std::strcmp(e, "wave") == 0;
-  }();
-  return wave != 0;
-}
-
-// Blocks of a hop launch over `sites` sites: one per `threads` sites, or, in
-// the wave mode, at most as many as the SMs hold at once (the occupancy of
-// this kernel and block size, queried once per kernel and block size).
-template <typename K>
-int hop_grid(K kernel, int threads, long sites) {
-  const int need = blocks_for(sites, threads);
-  if (!hop_grid_wave()) return need;
-  static std::map<std::pair<const void*, int>, int> per_sm;
-  const auto key = std::make_pair(reinterpret_cast<const void*>(kernel), threads);
-  auto it = per_sm.find(key);
-  if (it == per_sm.end()) {
-    int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, threads, 0) != cudaSuccess || n < 1) {
-      cudaGetLastError();
-      n = 0;
-    }
-    it = per_sm.emplace(key, n).first;
-  }
-  if (it->second == 0) return need;
-  const long wave = long(it->second) * rt().num_sms;
-  return int(need < wave ? need : wave);
-}
-
 template <int HB>
 void launch_mx_doe_t(int threads, const MixedBuffers& B, const MixScal* sc, cudaStream_t st) {
   const Geom& g = rt().g;
+  const int nb = blocks_for(g.sizeh, threads);
   with_sloppy_links(B, [&](const auto& u) {
     typedef typename std::decay<decltype(u)>::type LV;
     if (B.ph32_mode == PH_SIGN8)
-      launch_pdl(k_mx_doe<PH_SIGN8, LV, HB>, hop_grid(k_mx_doe<PH_SIGN8, LV, HB>, threads, g.sizeh), threads, st,
-                 g, u, B.ph32, B.p, B.t, sc);
-    else launch_pdl(k_mx_doe<PH_ANGLE, LV, HB>, hop_grid(k_mx_doe<PH_ANGLE, LV, HB>, threads, g.sizeh), threads,
-                    st, g, u, B.ph32, B.p, B.t, sc);
+      launch_pdl(k_mx_doe<PH_SIGN8, LV, HB>, nb, threads, st, g, u, B.ph32, B.p, B.t, sc);
+    else launch_pdl(k_mx_doe<PH_ANGLE, LV, HB>, nb, threads, st, g, u, B.ph32, B.p, B.t, sc);
   });
 }
 
@@ -403,12 +361,10 @@ void launch_mx_doe(HopShape sh, const MixedBuffers& B, const MixScal* sc, cudaSt
   else launch_mx_doe_t<1>(sh.threads, B, sc, st);
 }
 
-int mx_deo_blocks();
-
 template <int HB>
 void launch_mx_deo_dot_t(const MixedBuffers& B, MixScal* sc, ReduceWs ws, cudaStream_t st) {
   const Geom& g = rt().g;
-  const int nb = mx_deo_blocks();
+  const int nb = blocks_for(g.sizeh, MX_THREADS);
   with_sloppy_links(B, [&](const auto& u) {
     typedef typename std::decay<decltype(u)>::type LV;
     if (B.ph32_mode == PH_SIGN8)
@@ -423,10 +379,8 @@ void launch_mx_deo_dot(HopShape sh, const MixedBuffers& B, MixScal* sc, ReduceWs
   else launch_mx_deo_dot_t<1>(B, sc, ws, st);
 }
 
-// blocks of the k_mx_deo_dot launch (the reductions' partial sums): the same
-// for every hops-in-flight variant, so the autotuner's choice never changes
-// the summation order of <p, Ap>
-int mx_deo_blocks() { return hop_grid(k_mx_deo_dot<PH_SIGN8, LinkQ16, 1>, MX_THREADS, rt().g.sizeh); }
+// blocks of the k_mx_deo_dot launch (the reductions' partial sums)
+int mx_deo_blocks() { return blocks_for(rt().g.sizeh, MX_THREADS); }
 
 int doe_variant(const MixedBuffers& B) { return (B.ph32_mode == PH_SIGN8) + 2 * (B.q16 != 0); }
 

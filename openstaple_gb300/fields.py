@@ -61,6 +61,14 @@ def gaussian_vec3(dims, seed: int, stream: int = 7) -> np.ndarray:
     return (g[0::2] + 1j * g[1::2]).reshape(3, sh).copy()
 
 
+def z2_noise_vec3(dims, seed: int, stream: int = 11) -> np.ndarray:
+    """Z2 noise per half-lattice site and colour: +1 or -1 with probability
+    1/2 each, imaginary part zero, as the noise vectors of the fermionic
+    measurements (random_assignement.c:215-250).  complex128 (3, sizeh)."""
+    sh = sizeh(dims)
+    return np.where(uniforms(seed, 3 * sh, stream) < 0.5, 1.0, -1.0).reshape(3, sh).astype(np.complex128)
+
+
 def random_su3_links(dims, seed: int, eps: float = 0.3, stream: int = 1, chunk: int = 1 << 20) -> np.ndarray:
     """U = exp(i eps H) per link, H Gaussian traceless Hermitian.
 

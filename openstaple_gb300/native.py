@@ -152,6 +152,7 @@ SIGNATURES = {
     "find_min_max_eigenvalue_soloopenacc": (None, [_P, C.POINTER(FermParam), _P, _P, _P, _P, _P]),
     "inverter_mixed_precision": (_I, [InverterPackage, C.POINTER(FermParam), _P, _P, _D, _I, _D, C.POINTER(_I)]),
     "inverter_wrapper": (_I, [InverterPackage, C.POINTER(FermParam), _P, _P, _D, _I, _D, _I]),
+    "eo_inversion": (None, [InverterPackage, C.POINTER(FermParam), _D, _I, _P, _P, _P, _P, _P, _P]),
     "convergence_messages": (None, [_I, _I]),
     "ostaple_invert_mixed": (_I, [_P, _P, _D, _D, _P, _P, _D, _I, _I, _D, C.POINTER(_I), C.POINTER(_D),
                                   C.POINTER(_I)]),

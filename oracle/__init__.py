@@ -111,6 +111,15 @@ class Oracle:
         st = self.L.orc_cg(_p(u), _p(ph), mass, _p(x), _p(b), res, max_cg, shift, restart, C.byref(n))
         return st, n.value, x
 
+    def eo_inversion(self, u, ph, mass, in_e, in_o, res, max_cg=10000):
+        """D (out_e, out_o) = (in_e, in_o) by even/odd reduction
+        (Meas/ferm_meas.c:50-71): out_e = (M^+M)^-1 (m in_e - D_eo in_o) by
+        the FP64 CG from a zero guess, out_o = (in_o - D_oe out_e) / m."""
+        phi_e = mass * in_e - self.Deo(u, in_o, ph)
+        st, n, out_e = self.cg(u, ph, mass, phi_e, res, max_cg=max_cg)
+        out_o = (in_o - self.Doe(u, out_e, ph)) / mass
+        return st, n, out_e, out_o
+
     def cgm(self, u, ph, mass, shifts, b, res, max_cg=10000):
         shifts = np.ascontiguousarray(shifts, dtype=np.float64)
         xs = np.zeros((len(shifts), 3, self.sizeh), np.complex128)
