@@ -341,6 +341,23 @@ void rationalapprox_save(const char *nomefile, RationalApprox *rational_approx);
 void rescale_rational_approximation(RationalApprox *in, RationalApprox *out, double *minmax);
 void renormalize_rational_approximation(RationalApprox *in, RationalApprox *out);
 double rational_approx_evaluate(RationalApprox *in, double x);
+/* The library's own generator of these approximations (host code, no GPU).
+ * The reference generates .REMEZ files with a separate offline program over
+ * GMP multiprecision (RationalApprox/rationalapprox_calc.cc:20-95,
+ * Remez/alg_remez.cc); this is a new implementation in long double
+ * arithmetic, with no counterpart as a library function.  It computes the
+ * best relative-error approximation of x^|num/den| of order approx_order on
+ * [lambda_min, 1] by the Remez exchange and writes RA_a0, RA_a, RA_b (the
+ * partial fractions of r, or of 1/r for a negative exponent, poles
+ * ascending), error and lambda_max = 1.  Needs 0 < |num/den| < 1.  Returns 0,
+ * -3 for bad arguments, -15 when the exchange does not converge, -16 when
+ * the order is so high that its error is near the rounding level. */
+int ostaple_remez_approximation(RationalApprox *approx);
+/* The reference driver's order loop around it: the order guessed as
+ * log(goal) log(lambda_min)/19 + 2 (or fixed_order if > 0), raised by one
+ * until error <= goal_error; exponent_num, exponent_den and lambda_min are
+ * read from approx. */
+int ostaple_remez_generate(RationalApprox *approx, double goal_error, int fixed_order);
 
 void recombine_shifted_vec3_to_vec3(const vec3_soa *in_shifted, const vec3_soa *in, vec3_soa *out,
                                     const RationalApprox *approx);

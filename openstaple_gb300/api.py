@@ -375,6 +375,23 @@ def gauge_action(u, beta: float) -> dict:
 
 
 # ---- batched solvers ----
+def remez(exponent_num: int, exponent_den: int, lambda_min: float, order: int = 0,
+          goal_error: float | None = None) -> RationalApprox:
+    """The best relative-error rational approximation of x^(num/den) on
+    [lambda_min, 1] from the library's generator: of the given order, or of
+    the smallest order (starting from the reference driver's guess) whose
+    error is at most goal_error.  Returns the filled RationalApprox."""
+    ra = RationalApprox()
+    ra.exponent_num, ra.exponent_den, ra.lambda_min = int(exponent_num), int(exponent_den), float(lambda_min)
+    if goal_error is None:
+        ra.approx_order = int(order)
+        rc = lib().ostaple_remez_approximation(C.byref(ra))
+    else:
+        rc = lib().ostaple_remez_generate(C.byref(ra), float(goal_error), int(order))
+    check(rc, "ostaple_remez")
+    return ra
+
+
 def eo_inversion(ip, fp, res: float, max_cg: int, in_e, in_o, out_e, out_o, phi_e, phi_o) -> None:
     """Full-D inversion by even/odd reduction (Meas/ferm_meas.c:50-71)."""
     lib().eo_inversion(ip, C.byref(fp), res, max_cg, ptr(in_e), ptr(in_o), ptr(out_e), ptr(out_o), ptr(phi_e),

@@ -148,6 +148,8 @@ SIGNATURES = {
     "rescale_rational_approximation": (None, [C.POINTER(RationalApprox), C.POINTER(RationalApprox), _P]),
     "renormalize_rational_approximation": (None, [C.POINTER(RationalApprox), C.POINTER(RationalApprox)]),
     "rational_approx_evaluate": (_D, [C.POINTER(RationalApprox), _D]),
+    "ostaple_remez_approximation": (_I, [C.POINTER(RationalApprox)]),
+    "ostaple_remez_generate": (_I, [C.POINTER(RationalApprox), _D, _I]),
     "ker_find_min_eigenvalue_openacc": (_D, [_P, C.POINTER(FermParam), _P, _P, _P, _D]),
     "find_min_max_eigenvalue_soloopenacc": (None, [_P, C.POINTER(FermParam), _P, _P, _P, _P, _P]),
     "inverter_mixed_precision": (_I, [InverterPackage, C.POINTER(FermParam), _P, _P, _D, _I, _D, C.POINTER(_I)]),

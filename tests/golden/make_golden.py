@@ -7,7 +7,7 @@ Run from the repository root where the reference source tree is available
 (its path as the first argument, or in OSTAPLE_REFERENCE), optionally naming
 the fixture groups to write (default: all):
 
-    python tests/golden/make_golden.py /path/to/reference [dirac] [gauge] [config2] [hmc] [rhmc]
+    python tests/golden/make_golden.py /path/to/reference [dirac] [gauge] [config2] [hmc] [rhmc] [remez]
 
 * dirac   -- dirac_<dims>.npz: D_eo/D_oe, M^+M, CG, CG-M, eigenvalue bounds;
 * gauge   -- gauge_<dims>_e<eps>.npz: staples, Q_A, stout levels,
@@ -20,7 +20,10 @@ the fixture groups to write (default: all):
   (gauge staples and force, plaquette and rectangle sums, 1/2 tr P^2, the
   momentum kick, the link update, two multistep_2MN_gauge calls);
 * rhmc    -- rhmc_md_4x4x4x4.npz: the reference's multistep_2MN_SOLOOPENACC
-  (molecular dynamics with a two-pseudofermion flavour and stout smearing).
+  (molecular dynamics with a two-pseudofermion flavour and stout smearing);
+* remez   -- remez_reference.json: every .REMEZ file the reference ships in
+  its current format (full-precision header), the outputs of its
+  multiprecision Remez program, for the library's own generator to match.
 
 Inputs are regenerated from seeds by openstaple_gb300.fields, whose
 counter-based generator is platform independent; the fixture also stores a
@@ -284,6 +287,20 @@ def write_rhmc(approx: dict) -> None:
     print("wrote rhmc md")
 
 
+def write_remez(ref: Path) -> None:
+    out = {}
+    for path in sorted([*ref.glob("saved_approxs/*.REMEZ"), *ref.glob("tools/test/ratapproxes/*.REMEZ")]):
+        txt = path.read_text()
+        if not re.search(r"Lambda Min:\s*[-+0-9.]+e", txt):   # the older fixed-point header
+            continue
+        d = parse_remez(path)
+        if d["error"] <= 0:
+            continue
+        out[str(path.relative_to(ref))] = d
+    (HERE / "remez_reference.json").write_text(json.dumps(out, indent=1))
+    print("wrote remez", len(out))
+
+
 def main(refroot: str, groups) -> None:
     ref = Path(refroot)
     os.environ["OSTAPLE_REFERENCE"] = str(ref)
@@ -297,14 +314,16 @@ def main(refroot: str, groups) -> None:
         write_config2(approx)
     if "hmc" in groups:
         write_hmc(approx)
+    if "remez" in groups:
+        write_remez(ref)
     if "rhmc" in groups:
         write_rhmc(approx)
 
 
 if __name__ == "__main__":
     args = sys.argv[1:]
-    root = args.pop(0) if args and not args[0] in ("dirac", "gauge", "config2", "hmc", "rhmc") else os.environ.get(
+    root = args.pop(0) if args and not args[0] in ("dirac", "gauge", "config2", "hmc", "rhmc", "remez") else os.environ.get(
         "OSTAPLE_REFERENCE")
     if not root:
-        sys.exit("usage: make_golden.py /path/to/reference [dirac] [gauge] [config2] [hmc] [rhmc]")
-    main(root, set(args) or {"dirac", "gauge", "config2", "hmc", "rhmc"})
+        sys.exit("usage: make_golden.py /path/to/reference [dirac] [gauge] [config2] [hmc] [rhmc] [remez]")
+    main(root, set(args) or {"dirac", "gauge", "config2", "hmc", "rhmc", "remez"})
