@@ -131,6 +131,10 @@ def parse_args():
                     help="learned: flexible CG preconditioned by the network, trained before the timed region "
                          "on solver-produced pairs")
     ap.add_argument("--train-epochs", type=int, default=150)
+    ap.add_argument("--pairs", type=int, default=8,
+                    help="training pairs of the learned preconditioner (solved by the batched solver, 8 at a time)")
+    ap.add_argument("--pair-res", type=float, default=None,
+                    help="FP64 true residual of the training solutions (default: --res)")
     ap.add_argument("--rhs", type=int, default=1,
                     help="right-hand sides per step; >1 solves them together with the batched solver")
     ap.add_argument("--links", choices=("q16", "f32"), default="q16",
@@ -462,25 +466,49 @@ def main():
     if args.solver == "learned":
         # training pairs (b_i, x_i) from the batched solver, then GPU training
         from openstaple_gb300 import fields as F
-        tb = np.stack([F.gaussian_vec3(dims, args.seed + 17 * rank + 500 + k) for k in range(8)])
-        tx = lat.vec3(8)
-        lat.present(tb)
-        lat.present(tx)
+        npairs = max(1, args.pairs)
+        pair_res = args.pair_res or args.res
+        # sources drawn on the device (the host generator's numbers) and
+        # solutions starting from zero: the host arrays are never touched
+        tb = np.empty((npairs, 3, lat.sizeh), np.complex128)
+        tx = np.empty((npairs, 3, lat.sizeh), np.complex128)
+        lat.present(tb, copy=False)
+        lat.present(tx, copy=False)
+        for k in range(npairs):
+            api.check(L.ostaple_gaussian_vec3(tb[k].ctypes.data, args.seed + 17 * rank + 500 + k, 7),
+                      "ostaple_gaussian_vec3")
         t0 = time.perf_counter()
-        api.invert_mixed_batch(u, ph, args.mass, tx, tb, None, args.res, 100000, args.delta)
+        for k0 in range(0, npairs, 8):
+            k1 = min(npairs, k0 + 8)
+            rp = api.invert_mixed_batch(u, ph, args.mass, tx[k0:k1], tb[k0:k1], None, pair_res, 100000, args.delta)
+            assert rp["status"] == 1, "training pair solve failed"
         t1 = time.perf_counter()
         api.net_init(11, 0.05)
         hist = api.net_train(u, ph, args.mass, tb, tx, args.train_epochs, 3e-3)
         t2 = time.perf_counter()
-        learned = {"pairs": 8, "pair_generation_s": t1 - t0, "epochs": args.train_epochs, "training_s": t2 - t1,
+        learned = {"pairs": npairs, "pair_residual": pair_res, "pair_generation_s": t1 - t0,
+                   "epochs": args.train_epochs, "training_s": t2 - t1,
                    "loss_first": float(hist[0]), "loss_last": float(hist[-1])}
         lat.release(tb)
         lat.release(tx)
+        del tb, tx
+        # the mixed-precision CG alone on the same system, for comparison
+        tm = []
+        for _ in range(2):
+            L.set_vec3_soa_to_zero(x.ctypes.data)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record(stream)
+            rm = api.invert_mixed(u, ph, args.mass, 0.0, x, b, args.res, 100000, args.every, args.delta)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            tm.append(e0.elapsed_time(e1))
+        learned["mixed_cg"] = {"ms": min(tm), "iterations": int(rm["iters"]), "status": int(rm["status"])}
 
     def solve():
         if args.solver == "learned":
             L.set_vec3_soa_to_zero(x.ctypes.data)
-            r = api.invert_learned(u, ph, args.mass, 0.0, x, b, args.res, 5000)
+            r = api.invert_learned(u, ph, args.mass, 0.0, x, b, args.res, 100000)
             learned["used_fallback"] = r["used_fallback"]
             return dict(status=r["status"], iters=r["iters"], true_res=r["true_res"], n_reliable=-1)
         if nrhs > 1:
@@ -595,7 +623,7 @@ def main():
             for a in (ue, phe, be, xe):
                 lat.update_device(a)
             if args.solver == "learned":
-                api.invert_learned(ue, phe, args.mass, 0.0, xe, be, args.res, 5000)
+                api.invert_learned(ue, phe, args.mass, 0.0, xe, be, args.res, 100000)
             elif nrhs > 1:
                 api.invert_mixed_batch(ue, phe, args.mass, xe, be, None, args.res, 100000, args.delta)
             else:

@@ -525,6 +525,13 @@ int ostaple_pure_gauge_hmc(su3_soa *u, double beta, int ntraj, int no_md, int ga
 /* Gaussian momenta on the device from (seed, stream); the same counter-based
  * generator the host field helpers use */
 int ostaple_gauge_momenta(thmat_soa *mom, unsigned long long seed, unsigned long long stream);
+/* Fills a vec3_soa on the device with Gaussian complex numbers (real and
+ * imaginary parts of variance 1/2, as generate_vec3_soa_gauss,
+ * random_assignement.c:58-92) from the counter-based generator (seed,
+ * stream): element k takes the Box-Muller pair k, the same numbers as the
+ * host field helpers.  No reference counterpart (the reference draws on the
+ * host). */
+int ostaple_gaussian_vec3(vec3_soa *v, unsigned long long seed, unsigned long long stream);
 /* plaquette and rectangle sums and the action -beta/3 (C_ZERO P + C_ONE R) */
 int ostaple_gauge_action(const su3_soa *u, double beta, double *plaq_sum, double *rect_sum, double *action);
 

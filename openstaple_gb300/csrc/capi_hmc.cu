@@ -243,6 +243,14 @@ int ostaple_gauge_momenta(thmat_soa* mom, unsigned long long seed, unsigned long
   return error_code();
 }
 
+int ostaple_gaussian_vec3(vec3_soa* v, unsigned long long seed, unsigned long long stream) {
+  if (!require_init("ostaple_gaussian_vec3")) return -2;
+  double2* d = static_cast<double2*>(resolve(v, "v"));
+  if (!d) return -3;
+  launch_gen_vec3_gauss(d, seed, stream, S());
+  return error_code();
+}
+
 int ostaple_gauge_action(const su3_soa* u, double beta, double* plaq_sum, double* rect_sum, double* action) {
   if (!require_init("ostaple_gauge_action")) return -2;
   HmcLinks<double> l = links64(u, "u");

@@ -5,7 +5,8 @@
   max-norm), the plaquette, rectangle and momentum sums (1e-13), the momentum
   kick and the link update (1e-13), two multistep_2MN_gauge calls with
   initialize_md_global_variables (1e-12).
-* The device momentum generator against the host field helpers (1e-15).
+* The device momentum and Gaussian-vector generators against the host field
+  helpers (1e-15).
 * Properties of whole trajectories of the link generator (FP64 and FP32
   molecular dynamics): reversibility of the FP64 integrator to 1e-11, energy
   conservation improving with the step size, FP32 against FP64 molecular
@@ -97,6 +98,16 @@ def test_device_momenta_equal_the_host_generator(lat_factory):
     assert relerr(lat.update_host(mom), F.gauge_momenta(dims, 77, 5)) <= 1e-15
     # 1/2 tr P^2 of Gaussian momenta: 4 per link on average (8 deviates of variance 1/2)
     assert abs(api.momenta_action(mom) / (8 * lat.sizeh) - 4.0) < 0.1
+
+
+def test_device_gaussian_vectors_equal_the_host_generator(lat_factory):
+    from openstaple_gb300.native import lib
+    dims = (4, 6, 8, 10)
+    lat = lat_factory(dims)
+    v = lat.vec3()
+    lat.present(v, copy=False)
+    assert lib().ostaple_gaussian_vec3(v.ctypes.data, 123, 7) == 0
+    assert relerr(lat.update_host(v), F.gaussian_vec3(dims, 123, 7)) <= 1e-15
 
 
 def _md_trajectory(lat, u, mom, stap, ip, beta, no_md, gs, t):
