@@ -152,6 +152,68 @@ k_mx_deo_dot(Geom g, LV u, const void* __restrict__ ph, const float2* __restrict
   }
 }
 
+// Staged variants of the two hops (16-bit links and sign bytes only): all
+// loads of a site's eight hops in flight at once through cp.async
+// (dslash.cuh), links and signs issued before the programmatic wait.  Same
+// arithmetic as k_mx_doe / k_mx_deo_dot: the same bits.
+__global__ void __launch_bounds__(256)
+k_mx_doe_st(Geom g, LinkQ16 u, const void* __restrict__ ph, const float2* __restrict__ p, float2* __restrict__ t,
+            const MixScal* sc) {
+  extern __shared__ __align__(16) unsigned char stage_smem[];
+  if (halted(sc)) return;
+  const HopStage st(stage_smem, blockDim.x, threadIdx.x);
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool live = idx < g.sizeh;
+  int fwd[4], bwd[4];
+  unsigned char sb[8];
+  if (live) stage_links<1>(g, u, static_cast<const unsigned char*>(ph), idx, fwd, bwd, sb, st);
+  pdl_wait();               // p from k_mx_pupdate
+  pdl_trigger();
+  if (live) stage_vectors(p, g.sizeh, idx, fwd, bwd, st);
+  cp_async_wait_all();
+  if (!live) return;
+  float2 aux[3];
+  hop_fb_staged(sb, st, aux);
+#pragma unroll
+  for (int c = 0; c < 3; ++c) t[c * long(g.sizeh) + idx] = make_float2(0.5f * aux[c].x, 0.5f * aux[c].y);
+}
+
+__global__ void __launch_bounds__(MX_THREADS)
+k_mx_deo_dot_st(Geom g, LinkQ16 u, const void* __restrict__ ph, const float2* __restrict__ t,
+                const float2* __restrict__ p, float2* __restrict__ s, MixScal* sc, ReduceWs ws) {
+  extern __shared__ __align__(16) unsigned char stage_smem[];
+  if (halted(sc)) return;
+  const HopStage st(stage_smem, blockDim.x, threadIdx.x);
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool live = idx < g.sizeh;
+  int fwd[4], bwd[4];
+  unsigned char sb[8];
+  if (live) stage_links<0>(g, u, static_cast<const unsigned char*>(ph), idx, fwd, bwd, sb, st);
+  pdl_wait();               // t from k_mx_doe
+  pdl_trigger();
+  if (live) stage_vectors(t, g.sizeh, idx, fwd, bwd, st);
+  cp_async_wait_all();
+  float v[1] = {0.0f};
+  if (live) {
+    const float m2 = float(sc->m2);
+    float2 aux[3];
+    hop_fb_staged(sb, st, aux);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const long k = c * long(g.sizeh) + idx;
+      float2 pv = p[k];
+      float2 r = make_float2(fmaf(pv.x, m2, -0.5f * aux[c].x), fmaf(pv.y, m2, -0.5f * aux[c].y));
+      s[k] = r;
+      v[0] = fmaf(pv.x, r.x, fmaf(pv.y, r.y, v[0]));
+    }
+  }
+  double tot[1];
+  if (grid_reduce_f32w<1>(v, ws, tot)) {
+    sc->pAp = tot[0];
+    sc->alpha = sc->delta / tot[0];
+  }
+}
+
 // x_f += alpha p ; unless a reliable update is due: r -= alpha s, lambda = |r|^2,
 // beta = lambda / delta, delta = lambda.
 __global__ void k_mx_update(float4* __restrict__ xf, float4* __restrict__ r, const float4* __restrict__ p,
@@ -327,14 +389,32 @@ void fp64_mdagm(const MixedBuffers& B, double2* out, const double2* in, double2*
 }
 
 // Launch shapes the autotuner tries (the first is the default): block size
-// and hops in flight.  The block size of k_mx_deo_dot fixes the summation
-// order of <p, Ap>, so only its hops in flight are tuned.
+// and hops in flight, hb = STAGED for the cp.async variants (16-bit links
+// with sign bytes; with other link formats the default shape runs instead).
+// The block size of k_mx_deo_dot fixes the summation order of <p, Ap>, so
+// only its hops in flight are tuned.
 struct HopShape {
   int threads, hb;
 };
-static const HopShape kDoeShapes[7] = {{MX_THREADS, 1}, {256, 1}, {64, 1}, {MX_THREADS, 2},
-                                       {MX_THREADS, 4}, {256, 2}, {64, 2}};
-static const HopShape kDeoShapes[3] = {{MX_THREADS, 1}, {MX_THREADS, 2}, {MX_THREADS, 4}};
+constexpr int STAGED = 8;
+constexpr int N_DOE_SHAPES = 9, N_DEO_SHAPES = 4;
+static const HopShape kDoeShapes[N_DOE_SHAPES] = {{MX_THREADS, 1}, {256, 1}, {64, 1}, {MX_THREADS, 2},
+                                                  {MX_THREADS, 4}, {256, 2}, {64, 2}, {MX_THREADS, STAGED},
+                                                  {256, STAGED}};
+static const HopShape kDeoShapes[N_DEO_SHAPES] = {{MX_THREADS, 1}, {MX_THREADS, 2}, {MX_THREADS, 4},
+                                                  {MX_THREADS, STAGED}};
+
+template <typename K>
+void allow_stage_smem(K kernel, int threads) {
+  static int granted = 0;
+  const int bytes = threads * STAGE_BYTES_PER_THREAD;
+  if (bytes > granted && bytes > 48 * 1024) {
+    OST_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+    granted = bytes;
+  }
+}
+
+bool stageable(const MixedBuffers& B) { return B.q16 && B.ph32_mode == PH_SIGN8; }
 
 // Calls f with the view of the sloppy links the FP32 iteration reads.
 template <typename F>
@@ -356,6 +436,17 @@ void launch_mx_doe_t(int threads, const MixedBuffers& B, const MixScal* sc, cuda
 }
 
 void launch_mx_doe(HopShape sh, const MixedBuffers& B, const MixScal* sc, cudaStream_t st) {
+  if (sh.hb == STAGED) {
+    if (!stageable(B)) {
+      launch_mx_doe_t<1>(MX_THREADS, B, sc, st);
+      return;
+    }
+    const Geom& g = rt().g;
+    allow_stage_smem(k_mx_doe_st, sh.threads);
+    launch_pdl_smem(k_mx_doe_st, blocks_for(g.sizeh, sh.threads), sh.threads,
+                    size_t(sh.threads) * STAGE_BYTES_PER_THREAD, st, g, B.uq, B.ph32, B.p, B.t, sc);
+    return;
+  }
   if (sh.hb == 4) launch_mx_doe_t<4>(sh.threads, B, sc, st);
   else if (sh.hb == 2) launch_mx_doe_t<2>(sh.threads, B, sc, st);
   else launch_mx_doe_t<1>(sh.threads, B, sc, st);
@@ -374,6 +465,16 @@ void launch_mx_deo_dot_t(const MixedBuffers& B, MixScal* sc, ReduceWs ws, cudaSt
 }
 
 void launch_mx_deo_dot(HopShape sh, const MixedBuffers& B, MixScal* sc, ReduceWs ws, cudaStream_t st) {
+  if (sh.hb == STAGED) {
+    if (!stageable(B)) {
+      launch_mx_deo_dot_t<1>(B, sc, ws, st);
+      return;
+    }
+    const Geom& g = rt().g;
+    launch_pdl_smem(k_mx_deo_dot_st, blocks_for(g.sizeh, MX_THREADS), MX_THREADS,
+                    size_t(MX_THREADS) * STAGE_BYTES_PER_THREAD, st, g, B.uq, B.ph32, B.t, B.p, B.s, sc, ws);
+    return;
+  }
   if (sh.hb == 4) launch_mx_deo_dot_t<4>(B, sc, ws, st);
   else if (sh.hb == 2) launch_mx_deo_dot_t<2>(B, sc, ws, st);
   else launch_mx_deo_dot_t<1>(B, sc, ws, st);
@@ -386,12 +487,12 @@ int doe_variant(const MixedBuffers& B) { return (B.ph32_mode == PH_SIGN8) + 2 * 
 
 HopShape mx_doe_shape(const MixedBuffers& B) {
   const int pick = autotune_cached(TUNE_MX_DOE, rt().g.sizeh, doe_variant(B));
-  return kDoeShapes[pick > 0 && pick < 7 ? pick : 0];
+  return kDoeShapes[pick > 0 && pick < N_DOE_SHAPES ? pick : 0];
 }
 
 HopShape mx_deo_shape(const MixedBuffers& B) {
   const int pick = autotune_cached(TUNE_MX_DEO, rt().g.sizeh, doe_variant(B));
-  return kDeoShapes[pick > 0 && pick < 3 ? pick : 0];
+  return kDeoShapes[pick > 0 && pick < N_DEO_SHAPES ? pick : 0];
 }
 
 // Tunes the launch shapes of both hops once per lattice and link format
@@ -408,10 +509,11 @@ int tune_mx_hops(const MixedBuffers& B, cudaStream_t st) {
     h.delta = 1.0;
     MixScal* sc = static_cast<MixScal*>(autotune_scalars(&h, sizeof(h), st));
     if (sc) {
-      autotune_pick(TUNE_MX_DOE, sh, variant, 7, [&](int c) { launch_mx_doe(kDoeShapes[c], B, sc, st); }, st);
+      autotune_pick(TUNE_MX_DOE, sh, variant, N_DOE_SHAPES,
+                    [&](int c) { launch_mx_doe(kDoeShapes[c], B, sc, st); }, st);
       ReduceWs ws = reduce_ws(1, mx_deo_blocks());
-      autotune_pick(TUNE_MX_DEO, sh, variant, 3, [&](int c) { launch_mx_deo_dot(kDeoShapes[c], B, sc, ws, st); },
-                    st);
+      autotune_pick(TUNE_MX_DEO, sh, variant, N_DEO_SHAPES,
+                    [&](int c) { launch_mx_deo_dot(kDeoShapes[c], B, sc, ws, st); }, st);
     }
   }
   const int a = autotune_cached(TUNE_MX_DOE, sh, variant), b = autotune_cached(TUNE_MX_DEO, sh, variant);
