@@ -1,4 +1,5 @@
 // autotune.cu -- the launch-shape cache and its timing (see autotune.cuh).
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -15,7 +16,7 @@ namespace {
 
 struct Entry {
   int choice;
-  float us[8];
+  float us[12];
   int ncand;
 };
 
@@ -30,8 +31,9 @@ int g_forced = -1;    // >= 0: every tuned launch uses this candidate (tests)
 const char* kernel_name(int k) {
   switch (k) {
     case TUNE_MX_DOE:
-      return "k_mx_doe (threads per block, hops in flight) {128/1, 256/1, 64/1, 128/2, 128/4, 256/2, 64/2}";
-    case TUNE_MX_DEO: return "k_mx_deo_dot hops in flight {1, 2, 4}";
+      return "k_mx_doe (threads per block, hops in flight; s = all eight staged by cp.async) "
+             "{128/1, 256/1, 64/1, 128/2, 128/4, 256/2, 64/2, 128/s, 256/s}";
+    case TUNE_MX_DEO: return "k_mx_deo_dot hops in flight {1, 2, 4, s (all eight staged by cp.async)}";
     case TUNE_B_DOE: return "k_b_doe systems per thread {default, 1, 2, 4}";
     default: return "k_cgm_doe systems per thread {default, 1, 2, 4}";
   }
@@ -75,13 +77,25 @@ int autotune_pick(int kernel, long sizeh, int variant, int ncand, const std::fun
   auto it = table().find(key);
   if (it != table().end()) return it->second.choice;
   Entry e{};
-  e.ncand = ncand < 8 ? ncand : 8;
+  e.ncand = ncand < 12 ? ncand : 12;
   cudaEvent_t a, b;
   OST_CUDA(cudaEventCreate(&a));
   OST_CUDA(cudaEventCreate(&b));
   int best = 0;
+  const bool clean = error_code() == 0;
   for (int c = 0; c < e.ncand; ++c) {
     launch(c);
+    if (c > 0 && clean && error_code() != 0) {
+      // a candidate that this device refuses to launch (a launch-configuration
+      // error: nothing ran, the context is intact) is never picked
+      const cudaError_t le = cudaGetLastError();
+      if (le == cudaErrorInvalidValue || le == cudaErrorInvalidConfiguration ||
+          le == cudaErrorLaunchOutOfResources) {
+        clear_error();
+        e.us[c] = INFINITY;
+        continue;
+      }
+    }
     OST_CUDA(cudaEventRecord(a, st));
     for (int r = 0; r < 3; ++r) launch(c);
     OST_CUDA(cudaEventRecord(b, st));

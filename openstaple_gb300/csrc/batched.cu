@@ -446,6 +446,7 @@ struct BGraph {
 BGraph g_bgraph;
 cudaStream_t g_bcap = nullptr;
 BatchScal* g_bhost = nullptr;
+BatchScal* g_bflags = nullptr;   // two slots: the flags after the current chunk and after the chunk ahead
 
 void fp64_mdagm(const BatchBuffers& B, double2* out, const double2* in, double m2, cudaStream_t st) {
   DslashArgs<double> a;
@@ -552,6 +553,7 @@ BatchResult batched_mixed_cg(const BatchBuffers& B, const double* m2, double res
   if (!g_bcap) {
     OST_CUDA(cudaStreamCreateWithFlags(&g_bcap, cudaStreamNonBlocking));
     OST_CUDA(cudaMallocHost(&g_bhost, sizeof(BatchScal)));
+    OST_CUDA(cudaMallocHost(&g_bflags, 2 * sizeof(BatchScal)));
   }
   cudaEvent_t ev;
   OST_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
@@ -629,13 +631,40 @@ BatchResult batched_mixed_cg(const BatchBuffers& B, const double* m2, double res
     g_bgraph.epoch = runtime_epoch();
     g_bgraph.doe_pick = doe_pick;
   }
-  for (int guard = 0; guard < 1000000; ++guard) {
-    if (error_code()) break;
+  // Chunks run one ahead of the flag check (as in the single-system solver):
+  // the flags copied after chunk k are read while chunk k+1 runs.  When a
+  // system has halted (converged or a reliable update due), the chunk ahead
+  // did nothing for it; after that chunk has finished its flags are
+  // discarded and the pipeline restarts behind the host's work.
+  static cudaEvent_t flag_ev[2] = {nullptr, nullptr};
+  for (int k = 0; k < 2; ++k)
+    if (!flag_ev[k]) OST_CUDA(cudaEventCreateWithFlags(&flag_ev[k], cudaEventDisableTiming));
+  auto launch_chunk = [&](int slot) {
     OST_CUDA(cudaGraphLaunch(g_bgraph.exec, cs));
     g_kernel_launches += 4ull * chunk;
-    OST_CUDA(cudaMemcpyAsync(g_bhost, sc, sizeof(BatchScal), cudaMemcpyDeviceToHost, cs));
-    OST_CUDA(cudaStreamSynchronize(cs));
-    BatchScal h = *g_bhost;
+    OST_CUDA(cudaMemcpyAsync(g_bflags + slot, sc, sizeof(BatchScal), cudaMemcpyDeviceToHost, cs));
+    OST_CUDA(cudaEventRecord(flag_ev[slot], cs));
+  };
+  int cur = 0;
+  bool primed = false;
+  for (int guard = 0; guard < 1000000; ++guard) {
+    if (error_code()) break;
+    if (!primed) {
+      launch_chunk(cur);
+      primed = true;
+    }
+    launch_chunk(cur ^ 1);
+    OST_CUDA(cudaEventSynchronize(flag_ev[cur]));
+    BatchScal h = g_bflags[cur];
+    bool halted_any = false;
+    for (int k = 0; k < NSY; ++k)
+      if (!finished[k] && (h.need_rel[k] || h.done[k])) halted_any = true;
+    if (!halted_any) {
+      cur ^= 1;
+      continue;
+    }
+    OST_CUDA(cudaEventSynchronize(flag_ev[cur ^ 1]));
+    primed = false;
     bool all = true;
     for (int k = 0; k < NSY; ++k) {
       if (finished[k]) continue;

@@ -416,11 +416,13 @@ static const HopShape kDoeShapes[N_DOE_SHAPES] = {{MX_THREADS, 1}, {256, 1}, {64
 static const HopShape kDeoShapes[N_DEO_SHAPES] = {{MX_THREADS, 1}, {MX_THREADS, 2}, {MX_THREADS, 4},
                                                   {MX_THREADS, STAGED}};
 
+// The staged kernels' dynamic shared memory plus the reduction's static
+// shared memory exceed the 48 KB a kernel gets without opting in.
 template <typename K>
 void allow_stage_smem(K kernel, int threads) {
   static int granted = 0;
   const int bytes = threads * STAGE_BYTES_PER_THREAD;
-  if (bytes > granted && bytes > 48 * 1024) {
+  if (bytes > granted) {
     OST_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
     granted = bytes;
   }
@@ -483,6 +485,7 @@ void launch_mx_deo_dot(HopShape sh, const MixedBuffers& B, MixScal* sc, ReduceWs
       return;
     }
     const Geom& g = rt().g;
+    allow_stage_smem(k_mx_deo_dot_st, MX_THREADS);
     launch_pdl_smem(k_mx_deo_dot_st, blocks_for(g.sizeh, MX_THREADS), MX_THREADS,
                     size_t(MX_THREADS) * STAGE_BYTES_PER_THREAD, st, g, B.uq, B.ph32, B.t, B.p, B.s, sc, ws);
     return;
@@ -556,7 +559,7 @@ MixedResult mixed_cg(const MixedBuffers& B, const MixedOptions& o, MixScal* sc, 
   const long n = 3L * g.sizeh;
   if (!g_cap) {
     OST_CUDA(cudaStreamCreateWithFlags(&g_cap, cudaStreamNonBlocking));
-    OST_CUDA(cudaMallocHost(&g_host, sizeof(MixScal)));
+    OST_CUDA(cudaMallocHost(&g_host, 2 * sizeof(MixScal)));
   }
   // order the private stream after the caller's stream
   cudaEvent_t ev;
@@ -632,13 +635,37 @@ MixedResult mixed_cg(const MixedBuffers& B, const MixedOptions& o, MixScal* sc, 
 
   const long n4 = n / 2;
   const double res2 = o.res * o.res * bn;
-  for (int guard = 0; guard < 1000000; ++guard) {
-    if (error_code()) break;
+  // Chunks run one ahead of the flag check: the flags copied after chunk k
+  // are read while chunk k+1 runs, so the GPU does not wait for the host
+  // between chunks.  Once the recursion has halted (converged, or a reliable
+  // update is due) every kernel of the chunk launched ahead returns at once;
+  // that chunk's flags are discarded.
+  static cudaEvent_t flag_ev[2] = {nullptr, nullptr};
+  for (int k = 0; k < 2; ++k)
+    if (!flag_ev[k]) OST_CUDA(cudaEventCreateWithFlags(&flag_ev[k], cudaEventDisableTiming));
+  auto launch_chunk = [&](int slot) {
     OST_CUDA(cudaGraphLaunch(g_cache.exec, cs));
     g_kernel_launches += 4ull * o.chunk;
-    OST_CUDA(cudaMemcpyAsync(g_host, sc, sizeof(MixScal), cudaMemcpyDeviceToHost, cs));
-    OST_CUDA(cudaStreamSynchronize(cs));
-    const MixScal h = *g_host;
+    OST_CUDA(cudaMemcpyAsync(g_host + slot, sc, sizeof(MixScal), cudaMemcpyDeviceToHost, cs));
+    OST_CUDA(cudaEventRecord(flag_ev[slot], cs));
+  };
+  int cur = 0;
+  bool primed = false;
+  for (int guard = 0; guard < 1000000; ++guard) {
+    if (error_code()) break;
+    if (!primed) {
+      launch_chunk(cur);
+      primed = true;
+    }
+    launch_chunk(cur ^ 1);
+    OST_CUDA(cudaEventSynchronize(flag_ev[cur]));
+    const MixScal h = g_host[cur];
+    if (!h.need_rel && !h.done) {
+      cur ^= 1;   // the chunk ahead becomes the current one
+      continue;
+    }
+    OST_CUDA(cudaEventSynchronize(flag_ev[cur ^ 1]));
+    primed = false;
     if (h.need_rel) {
       k_mx_accumulate<<<8 * rt().num_sms, 256, 0, cs>>>(B.x, B.xf, n);
       OST_LAUNCH_CHECK();
