@@ -962,6 +962,71 @@ __global__ void k_cgm_copy_f(float2* __restrict__ dst, const float2* __restrict_
   for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n; i += long(gridDim.x) * blockDim.x) dst[i] = src[i];
 }
 
+// The loop test of the device-side CG-M loop: continue while any
+// right-hand side is still iterating.  trips counts the passes of the loop
+// body; at max_trips (beyond the iteration limit, which sets done by
+// itself) the loop stops and trips turns negative.
+__global__ void k_cgm_continue(cudaGraphConditionalHandle h, const CgmScal* sc, int* trips, int max_trips) {
+  int all = 1;
+  for (int r = 0; r < sc->nrhs; ++r) all &= (sc->done[r] != 0);
+  const int t = *trips + 1;
+  *trips = t;
+  if (!all && t >= max_trips) {
+    *trips = -t;
+    all = 1;
+  }
+  cudaGraphSetConditional(h, all ? 0u : 1u);
+}
+
+// All iterations of the batched CG-M as one graph launch: a while node whose
+// body is `chunk` captured iterations followed by k_cgm_continue.  Returns
+// false (nothing launched, no error recorded) where the graph cannot be
+// built, and the caller runs its host-driven loop instead.
+template <typename Enq>
+bool cgm_device_loop(const Enq& enqueue_chunk, const CgmScal* sc, int* trips, int max_trips, int chunk,
+                     int* trips_out, cudaStream_t st) {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  bool ok = cudaGraphCreate(&graph, 0) == cudaSuccess;
+  cudaGraphConditionalHandle handle{};
+  if (ok) ok = cudaGraphConditionalHandleCreate(&handle, graph, 1, cudaGraphCondAssignDefault) == cudaSuccess;
+  cudaGraphNodeParams cp{};
+  cudaGraphNode_t node;
+  if (ok) {
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = handle;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    ok = cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &cp) == cudaSuccess;
+  }
+  if (ok) {
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    ok = cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) ==
+         cudaSuccess;
+    if (ok) {
+      const unsigned long long counted = g_kernel_launches;
+      enqueue_chunk();
+      k_cgm_continue<<<1, 1, 0, st>>>(handle, sc, trips, max_trips);
+      g_kernel_launches = counted;
+      ok = cudaStreamEndCapture(st, &body) == cudaSuccess;
+    }
+  }
+  if (ok) ok = cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess;
+  if (graph) cudaGraphDestroy(graph);
+  if (!ok) {
+    if (exec) cudaGraphExecDestroy(exec);
+    cudaGetLastError();
+    return false;
+  }
+  OST_CUDA(cudaMemsetAsync(trips, 0, sizeof(int), st));
+  OST_CUDA(cudaGraphLaunch(exec, st));
+  OST_CUDA(cudaMemcpyAsync(trips_out, trips, sizeof(int), cudaMemcpyDeviceToHost, st));
+  OST_CUDA(cudaStreamSynchronize(st));
+  cudaGraphExecDestroy(exec);
+  (void)chunk;
+  return true;
+}
+
 CgmBatchResult batched_cgm_f32(const CgmBatchBuffers& B, double mass2, const double* shifts, double res,
                                int max_iter, cudaStream_t st) {
   CgmBatchResult out;
@@ -1011,36 +1076,51 @@ CgmBatchResult batched_cgm_f32(const CgmBatchBuffers& B, double mass2, const dou
   }
   // capture a chunk of iterations once per call (the buffers change per call)
   const int chunk = 8;
-  cudaGraph_t graph;
-  cudaGraphExec_t exec;
-  const unsigned long long counted = g_kernel_launches;
-  OST_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-  for (int c = 0; c < chunk; ++c) {
-    switch (NR) {
-      case 1: enqueue_cgm_iteration<1>(B, sc, snap, st); break;
-      case 2: enqueue_cgm_iteration<2>(B, sc, snap, st); break;
-      case 3: enqueue_cgm_iteration<3>(B, sc, snap, st); break;
-      default: enqueue_cgm_iteration<4>(B, sc, snap, st); break;
+  auto enqueue_chunk = [&]() {
+    for (int c = 0; c < chunk; ++c) {
+      switch (NR) {
+        case 1: enqueue_cgm_iteration<1>(B, sc, snap, st); break;
+        case 2: enqueue_cgm_iteration<2>(B, sc, snap, st); break;
+        case 3: enqueue_cgm_iteration<3>(B, sc, snap, st); break;
+        default: enqueue_cgm_iteration<4>(B, sc, snap, st); break;
+      }
     }
-  }
-  OST_CUDA(cudaStreamEndCapture(st, &graph));
-  g_kernel_launches = counted;
-  OST_CUDA(cudaGraphInstantiate(&exec, graph, 0));
-  cudaGraphDestroy(graph);
-  int dn[BATCH_MAX];
-  for (int guard = 0; guard < 1000000 && !error_code(); ++guard) {
-    OST_CUDA(cudaGraphLaunch(exec, st));
-    g_kernel_launches += 5ull * chunk;
-    OST_CUDA(cudaMemcpyAsync(dn, sc->done, NR * sizeof(int), cudaMemcpyDeviceToHost, st));
-    OST_CUDA(cudaStreamSynchronize(st));
-    bool all = true;
-    for (int r = 0; r < NR; ++r) all = all && dn[r];
-    if (all) break;
+  };
+  // the whole iteration on the device: one graph launch with a while node
+  int* trips = snap + 8;
+  const int max_trips = max_iter / chunk + 2;
+  int trips_h = 0;
+  out.device_loop = cgm_device_loop(enqueue_chunk, sc, trips, max_trips, chunk, &trips_h, st);
+  if (out.device_loop) {
+    const int passes = trips_h < 0 ? -trips_h : trips_h;
+    g_kernel_launches += (5ull * chunk + 1) * passes;
+    if (trips_h < 0) set_error(-15, "batched CG-M: the device loop stopped at its bound of %d passes", max_trips);
+  } else {
+    // host-driven: replay a captured chunk, poll the flags after each
+    cudaGraph_t graph;
+    cudaGraphExec_t exec;
+    const unsigned long long counted = g_kernel_launches;
+    OST_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    enqueue_chunk();
+    OST_CUDA(cudaStreamEndCapture(st, &graph));
+    g_kernel_launches = counted;
+    OST_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+    cudaGraphDestroy(graph);
+    int dn[BATCH_MAX];
+    for (int guard = 0; guard < 1000000 && !error_code(); ++guard) {
+      OST_CUDA(cudaGraphLaunch(exec, st));
+      g_kernel_launches += 5ull * chunk;
+      OST_CUDA(cudaMemcpyAsync(dn, sc->done, NR * sizeof(int), cudaMemcpyDeviceToHost, st));
+      OST_CUDA(cudaStreamSynchronize(st));
+      bool all = true;
+      for (int r = 0; r < NR; ++r) all = all && dn[r];
+      if (all) break;
+    }
+    cudaGraphExecDestroy(exec);
   }
   OST_CUDA(cudaMemcpyAsync(h, sc, sizeof(CgmScal), cudaMemcpyDeviceToHost, st));
   OST_CUDA(cudaStreamSynchronize(st));
   for (int r = 0; r < NR; ++r) out.iters[r] = h->iter[r];
-  cudaGraphExecDestroy(exec);
   cudaFreeHost(h);
   return out;
 }

@@ -77,6 +77,7 @@ struct CgmBatchBuffers {
 
 struct CgmBatchResult {
   int iters[BATCH_MAX];
+  bool device_loop;   // the iterations ran as one graph launch with a device-side while loop
 };
 
 CgmBatchResult batched_cgm_f32(const CgmBatchBuffers& B, double mass2, const double* shifts, double res,
