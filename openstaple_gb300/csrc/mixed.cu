@@ -384,7 +384,8 @@ MixScal* g_host = nullptr;
 
 bool same_key(const MixedBuffers& a, const MixedBuffers& b) {
   return a.u32 == b.u32 && a.ph32 == b.ph32 && a.ph32_mode == b.ph32_mode && a.u32_compact == b.u32_compact &&
-         a.r == b.r && a.p == b.p && a.s == b.s && a.xf == b.xf && a.t == b.t;
+         a.q16 == b.q16 && a.uq.a == b.uq.a && a.uq.b == b.uq.b && a.r == b.r && a.p == b.p && a.s == b.s &&
+         a.xf == b.xf && a.t == b.t;
 }
 
 void fp64_mdagm(const MixedBuffers& B, double2* out, const double2* in, double2* tmp, double m2, cudaStream_t st) {
@@ -551,6 +552,148 @@ void enqueue_iteration(const MixedBuffers& B, MixScal* sc, cudaStream_t st) {
   g_kernel_launches += 2;
 }
 
+// ---- the whole solve on the device ----
+// One graph launch runs the iteration until the FP32 recursion has converged:
+// a while node whose body is a captured chunk of iterations, then an if node
+// that performs a due reliable update, then the loop test.  The two tests are
+// single-thread kernels that set the nodes' conditions from the device
+// scalars; the loop is bounded by a pass count beyond the iteration limit.
+__global__ void k_mx_rel_test(cudaGraphConditionalHandle h_rel, const MixScal* sc) {
+  cudaGraphSetConditional(h_rel, (sc->need_rel && !sc->done) ? 1u : 0u);
+}
+
+__global__ void k_mx_loop_test(cudaGraphConditionalHandle h_loop, const MixScal* sc, int* trips, int max_trips) {
+  const int t = *trips + 1;
+  *trips = t;
+  int go = !sc->done;
+  if (go && t >= max_trips) {
+    *trips = -t;
+    go = 0;
+  }
+  cudaGraphSetConditional(h_loop, go ? 1u : 0u);
+}
+
+// the reliable update of the host loop below, as stream work
+void enqueue_reliable_update(const MixedBuffers& B, double m2, MixScal* sc, cudaStream_t cs) {
+  const long n = 3L * rt().g.sizeh, n4 = n / 2;
+  k_mx_accumulate<<<8 * rt().num_sms, 256, 0, cs>>>(B.x, B.xf, n);
+  OST_LAUNCH_CHECK();
+  if (B.use_df) df_mdagm(B.df, B.dfw, B.t64, B.x, m2, cs);
+  else fp64_mdagm(B, B.t64, B.x, B.t64b, m2, cs);
+  const int gr = reduce_grid(n);
+  k_mx_residual<<<gr, RED_THREADS, 0, cs>>>(B.b, B.t64, B.r64, B.r, B.p, B.s, n, sc, reduce_ws(3, gr), 1);
+  OST_LAUNCH_CHECK();
+  k_mx_pupdate<<<reduce_grid(n4), RED_THREADS, 0, cs>>>(reinterpret_cast<float4*>(B.p),
+                                                        reinterpret_cast<const float4*>(B.r), n4, sc, 0);
+  OST_LAUNCH_CHECK();
+}
+
+template <typename F>
+bool capture_into(cudaStream_t cs, cudaGraph_t* g, F&& f) {
+  if (cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return false;
+  f();
+  return cudaStreamEndCapture(cs, g) == cudaSuccess && *g;
+}
+
+struct LoopCache {
+  cudaGraphExec_t exec = nullptr;
+  MixedBuffers key{};
+  int chunk = 0, hop_shapes = -1, max_trips = 0;
+  double m2 = 0;
+  MixScal* sc = nullptr;
+  unsigned long long epoch = 0;
+};
+LoopCache g_loop;
+
+bool same_loop_key(const LoopCache& c, const MixedBuffers& B, const MixedOptions& o, MixScal* sc, int hop_shapes,
+                   int max_trips) {
+  return c.exec && same_key(c.key, B) && c.key.x == B.x && c.key.b == B.b && c.key.u64 == B.u64 &&
+         c.key.ph64 == B.ph64 && c.key.t64 == B.t64 && c.key.r64 == B.r64 && c.key.t64b == B.t64b &&
+         c.key.use_df == B.use_df && c.chunk == o.chunk && c.m2 == o.mass2 && c.sc == sc &&
+         c.hop_shapes == hop_shapes && c.max_trips == max_trips && c.epoch == runtime_epoch();
+}
+
+// The executable graph of the device loop (cached per buffers and options),
+// or nullptr where this device or driver cannot build it.
+cudaGraphExec_t device_loop(const MixedBuffers& B, const MixedOptions& o, MixScal* sc, int* trips, int max_trips,
+                            int hop_shapes, cudaStream_t cs) {
+  if (same_loop_key(g_loop, B, o, sc, hop_shapes, max_trips)) return g_loop.exec;
+  if (g_loop.exec) cudaGraphExecDestroy(g_loop.exec);
+  g_loop.exec = nullptr;
+  const unsigned long long counted = g_kernel_launches;   // building launches nothing
+  cudaGraph_t graph = nullptr, chunk_g = nullptr, rel_g = nullptr, test_g = nullptr;
+  cudaGraphConditionalHandle h_loop{}, h_rel{};
+  bool ok = cudaGraphCreate(&graph, 0) == cudaSuccess;
+  ok = ok && cudaGraphConditionalHandleCreate(&h_loop, graph, 1, cudaGraphCondAssignDefault) == cudaSuccess;
+  ok = ok && cudaGraphConditionalHandleCreate(&h_rel, graph, 0, cudaGraphCondAssignDefault) == cudaSuccess;
+  ok = ok && capture_into(cs, &chunk_g, [&] {
+    for (int k = 0; k < o.chunk; ++k) enqueue_iteration(B, sc, cs);
+    k_mx_rel_test<<<1, 1, 0, cs>>>(h_rel, sc);
+  });
+  ok = ok && capture_into(cs, &rel_g, [&] { enqueue_reliable_update(B, o.mass2, sc, cs); });
+  ok = ok && capture_into(cs, &test_g, [&] { k_mx_loop_test<<<1, 1, 0, cs>>>(h_loop, sc, trips, max_trips); });
+  cudaGraphNodeParams wp{};
+  cudaGraphNode_t wnode;
+  if (ok) {
+    wp.type = cudaGraphNodeTypeConditional;
+    wp.conditional.handle = h_loop;
+    wp.conditional.type = cudaGraphCondTypeWhile;
+    wp.conditional.size = 1;
+    ok = cudaGraphAddNode(&wnode, graph, nullptr, nullptr, 0, &wp) == cudaSuccess;
+  }
+  if (ok) {
+    cudaGraph_t body = wp.conditional.phGraph_out[0];
+    cudaGraphNode_t n1, n2, n3, n4;
+    cudaGraphNodeParams ip{};
+    ip.type = cudaGraphNodeTypeConditional;
+    ip.conditional.handle = h_rel;
+    ip.conditional.type = cudaGraphCondTypeIf;
+    ip.conditional.size = 1;
+    ok = cudaGraphAddChildGraphNode(&n1, body, nullptr, 0, chunk_g) == cudaSuccess;
+    ok = ok && cudaGraphAddNode(&n2, body, &n1, nullptr, 1, &ip) == cudaSuccess;
+    ok = ok && cudaGraphAddChildGraphNode(&n4, ip.conditional.phGraph_out[0], nullptr, 0, rel_g) == cudaSuccess;
+    ok = ok && cudaGraphAddChildGraphNode(&n3, body, &n2, 1, test_g) == cudaSuccess;
+  }
+  cudaGraphExec_t exec = nullptr;
+  if (ok) ok = cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess;
+  for (cudaGraph_t gph : {chunk_g, rel_g, test_g, graph})
+    if (gph) cudaGraphDestroy(gph);
+  g_kernel_launches = counted;
+  if (!ok) {
+    if (exec) cudaGraphExecDestroy(exec);
+    cudaGetLastError();
+    return nullptr;
+  }
+  g_loop.exec = exec;
+  g_loop.key = B;
+  g_loop.chunk = o.chunk;
+  g_loop.m2 = o.mass2;
+  g_loop.sc = sc;
+  g_loop.hop_shapes = hop_shapes;
+  g_loop.max_trips = max_trips;
+  g_loop.epoch = runtime_epoch();
+  return exec;
+}
+
+bool device_loop_enabled() {
+  static const int on = [] {
+    const char* e = std::getenv("OSTAPLE_DEVICE_LOOP");
+    return (e && std::strcmp(e, "0") == 0) ? 0 : 1;
+  }();
+  return on != 0;
+}
+
+__device__ int g_mx_trips;
+
+int* device_loop_trips() {
+  static int* p = nullptr;
+  if (!p && cudaGetSymbolAddress(reinterpret_cast<void**>(&p), g_mx_trips) != cudaSuccess) {
+    cudaGetLastError();
+    p = nullptr;
+  }
+  return p;
+}
+
 }  // namespace
 
 MixedResult mixed_cg(const MixedBuffers& B, const MixedOptions& o, MixScal* sc, cudaStream_t st) {
@@ -635,6 +778,62 @@ MixedResult mixed_cg(const MixedBuffers& B, const MixedOptions& o, MixScal* sc, 
 
   const long n4 = n / 2;
   const double res2 = o.res * o.res * bn;
+  // The recursion has converged: fold the FP32 correction in and measure the
+  // FP64 true residual.  Returns true when the solve is finished; otherwise
+  // the FP32 target is tightened and the iteration continues from the
+  // recomputed residual (the closing residual acts as a reliable update).
+  auto close_or_tighten = [&]() -> bool {
+    k_mx_accumulate<<<8 * rt().num_sms, 256, 0, cs>>>(B.x, B.xf, n);
+    OST_LAUNCH_CHECK();
+    fp64_mdagm(B, B.t64, B.x, B.t64b, o.mass2, cs);
+    int gr = reduce_grid(n);
+    // mode 1 recomputes r, resets last_max and re-evaluates done
+    k_mx_residual<<<gr, RED_THREADS, 0, cs>>>(B.b, B.t64, B.r64, B.r, B.p, B.s, n, sc, reduce_ws(3, gr), 1);
+    OST_LAUNCH_CHECK();
+    OST_CUDA(cudaMemcpyAsync(g_host, sc, sizeof(MixScal), cudaMemcpyDeviceToHost, cs));
+    OST_CUDA(cudaStreamSynchronize(cs));
+    const MixScal f = *g_host;
+    res.iters = f.iter;
+    res.n_reliable = f.n_rel - 1;   // the closing residual is not an update
+    res.true_res = std::sqrt(f.true_r2 / bn);
+    res.converged = f.true_r2 <= res2;
+    if (res.converged || !o.guarantee || f.iter >= o.max_iter) return true;
+    fp32_target *= 0.5;
+    MixScal upd = f;
+    upd.target2 = fp32_target * fp32_target * bn;
+    upd.done = (f.lambda <= upd.target2) ? 1 : 0;
+    OST_CUDA(cudaMemcpyAsync(sc, &upd, sizeof(MixScal), cudaMemcpyHostToDevice, cs));
+    k_mx_pupdate<<<reduce_grid(n4), RED_THREADS, 0, cs>>>(reinterpret_cast<float4*>(B.p),
+                                                          reinterpret_cast<const float4*>(B.r), n4, sc, 0);
+    OST_LAUNCH_CHECK();
+    return false;
+  };
+
+  // the iteration as one graph launch with its loop on the device
+  int* trips = device_loop_enabled() ? device_loop_trips() : nullptr;
+  const int max_trips = 2 * (o.max_iter / (o.chunk > 0 ? o.chunk : 1)) + 16;
+  cudaGraphExec_t loop = trips ? device_loop(B, o, sc, trips, max_trips, hop_shapes, cs) : nullptr;
+  if (loop) {
+    int* trips_h = reinterpret_cast<int*>(g_host + 1);
+    for (int round = 0; round < 64 && !error_code(); ++round) {
+      OST_CUDA(cudaMemsetAsync(trips, 0, sizeof(int), cs));
+      OST_CUDA(cudaGraphLaunch(loop, cs));
+      OST_CUDA(cudaMemcpyAsync(trips_h, trips, sizeof(int), cudaMemcpyDeviceToHost, cs));
+      OST_CUDA(cudaStreamSynchronize(cs));
+      const int passes = *trips_h < 0 ? -*trips_h : *trips_h;
+      g_kernel_launches += (4ull * o.chunk + 2) * passes;
+      if (*trips_h < 0) {
+        set_error(-15, "mixed CG: the device loop stopped at its bound of %d passes", max_trips);
+        break;
+      }
+      if (close_or_tighten()) break;
+    }
+    OST_CUDA(cudaEventRecord(ev, cs));
+    OST_CUDA(cudaStreamWaitEvent(st, ev, 0));
+    OST_CUDA(cudaEventDestroy(ev));
+    return res;
+  }
+
   // Chunks run one ahead of the flag check: the flags copied after chunk k
   // are read while chunk k+1 runs, so the GPU does not wait for the host
   // between chunks.  Once the recursion has halted (converged, or a reliable
@@ -682,32 +881,7 @@ MixedResult mixed_cg(const MixedBuffers& B, const MixedOptions& o, MixScal* sc, 
       continue;
     }
     if (h.done) {
-      // fold the FP32 correction in and measure the FP64 true residual
-      k_mx_accumulate<<<8 * rt().num_sms, 256, 0, cs>>>(B.x, B.xf, n);
-      OST_LAUNCH_CHECK();
-      fp64_mdagm(B, B.t64, B.x, B.t64b, o.mass2, cs);
-      int gr = reduce_grid(n);
-      // mode 1 recomputes r, resets last_max and re-evaluates done
-      k_mx_residual<<<gr, RED_THREADS, 0, cs>>>(B.b, B.t64, B.r64, B.r, B.p, B.s, n, sc, reduce_ws(3, gr), 1);
-      OST_LAUNCH_CHECK();
-      OST_CUDA(cudaMemcpyAsync(g_host, sc, sizeof(MixScal), cudaMemcpyDeviceToHost, cs));
-      OST_CUDA(cudaStreamSynchronize(cs));
-      const MixScal f = *g_host;
-      res.iters = f.iter;
-      res.n_reliable = f.n_rel - 1;   // the closing residual is not an update
-      res.true_res = std::sqrt(f.true_r2 / bn);
-      res.converged = f.true_r2 <= res2;
-      if (res.converged || !o.guarantee || f.iter >= o.max_iter) break;
-      // not there yet in FP64: tighten the FP32 target and continue from the
-      // recomputed residual (the closing residual acts as a reliable update)
-      fp32_target *= 0.5;
-      MixScal upd = f;
-      upd.target2 = fp32_target * fp32_target * bn;
-      upd.done = (f.lambda <= upd.target2) ? 1 : 0;
-      OST_CUDA(cudaMemcpyAsync(sc, &upd, sizeof(MixScal), cudaMemcpyHostToDevice, cs));
-      k_mx_pupdate<<<reduce_grid(n4), RED_THREADS, 0, cs>>>(reinterpret_cast<float4*>(B.p),
-                                                            reinterpret_cast<const float4*>(B.r), n4, sc, 0);
-      OST_LAUNCH_CHECK();
+      if (close_or_tighten()) break;
       continue;
     }
   }
