@@ -203,6 +203,13 @@ int ostaple_unpin_host(void *host);
  * truncated to len) and returns the full length.  No reference counterpart
  * (the reference's launch shapes are fixed at compile time). */
 int ostaple_autotune(int enable);
+/* 1 (default, unless OSTAPLE_DEVICE_LOOP=0 in the environment): the mixed
+ * solver and the batched multi-shift CG run their iterations as one CUDA
+ * graph launch whose loop and reliable-update decisions are taken on the
+ * device (conditional graph nodes); 0: the host replays a captured chunk of
+ * iterations and polls the solver's flags.  Both give the same bits.  No
+ * reference counterpart. */
+int ostaple_device_loop(int enable);
 int ostaple_autotune_report(char *buf, int len);
 
 /* ---- staggered Dirac operator (fermion_matrix.h:20-39) ----------------- */

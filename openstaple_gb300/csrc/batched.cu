@@ -1090,7 +1090,7 @@ CgmBatchResult batched_cgm_f32(const CgmBatchBuffers& B, double mass2, const dou
   int* trips = snap + 8;
   const int max_trips = max_iter / chunk + 2;
   int trips_h = 0;
-  out.device_loop = cgm_device_loop(enqueue_chunk, sc, trips, max_trips, chunk, &trips_h, st);
+  out.device_loop = device_loop_enabled() && cgm_device_loop(enqueue_chunk, sc, trips, max_trips, chunk, &trips_h, st);
   if (out.device_loop) {
     const int passes = trips_h < 0 ? -trips_h : trips_h;
     g_kernel_launches += (5ull * chunk + 1) * passes;

@@ -675,14 +675,6 @@ cudaGraphExec_t device_loop(const MixedBuffers& B, const MixedOptions& o, MixSca
   return exec;
 }
 
-bool device_loop_enabled() {
-  static const int on = [] {
-    const char* e = std::getenv("OSTAPLE_DEVICE_LOOP");
-    return (e && std::strcmp(e, "0") == 0) ? 0 : 1;
-  }();
-  return on != 0;
-}
-
 __device__ int g_mx_trips;
 
 int* device_loop_trips() {

@@ -19,6 +19,16 @@ static Runtime g_rt;
 static Geom g_host_geom{};
 unsigned long long g_kernel_launches = 0;
 
+int g_device_loop = -1;   // -1: the environment decides
+
+bool device_loop_enabled() {
+  if (g_device_loop < 0) {
+    const char* e = std::getenv("OSTAPLE_DEVICE_LOOP");
+    g_device_loop = (e && std::strcmp(e, "0") == 0) ? 0 : 1;
+  }
+  return g_device_loop != 0;
+}
+
 bool pdl_enabled() {
   static int on = -1;
   if (on < 0) {
@@ -121,6 +131,11 @@ static void free_workspace() {
 using namespace ost;
 
 extern "C" {
+
+int ostaple_device_loop(int enable) {
+  ost::g_device_loop = enable ? 1 : 0;
+  return 0;
+}
 
 int ostaple_init(int n0, int n1, int n2, int n3) {
   clear_error();

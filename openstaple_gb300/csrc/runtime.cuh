@@ -62,6 +62,11 @@ bool require_init(const char* who);
 // attribute.  OSTAPLE_PDL=0 in the environment launches without it.
 bool pdl_enabled();
 
+// Solvers run their iteration as one graph launch with a device-side loop
+// (conditional graph nodes) unless this is off: ostaple_device_loop(0), or
+// OSTAPLE_DEVICE_LOOP=0 in the environment.
+bool device_loop_enabled();
+
 template <typename... P, typename... A>
 void launch_pdl_smem(void (*kernel)(P...), int grid, int block, size_t smem, cudaStream_t st, A&&... args) {
   cudaLaunchConfig_t cfg{};

@@ -156,6 +156,7 @@ SIGNATURES = {
     "inverter_wrapper": (_I, [InverterPackage, C.POINTER(FermParam), _P, _P, _D, _I, _D, _I]),
     "eo_inversion": (None, [InverterPackage, C.POINTER(FermParam), _D, _I, _P, _P, _P, _P, _P, _P]),
     "ostaple_gaussian_vec3": (_I, [_P, C.c_ulonglong, C.c_ulonglong]),
+    "ostaple_device_loop": (_I, [_I]),
     "convergence_messages": (None, [_I, _I]),
     "ostaple_invert_mixed": (_I, [_P, _P, _D, _D, _P, _P, _D, _I, _I, _D, C.POINTER(_I), C.POINTER(_D),
                                   C.POINTER(_I)]),
