@@ -509,6 +509,12 @@ def autotune(enable: bool) -> None:
     lib().ostaple_autotune(1 if enable else 0)
 
 
+def autotune_force(candidate: int) -> None:
+    """Every tuned launch uses candidate shape `candidate` (0 = the default;
+    a kernel with fewer candidates uses its default): for tests."""
+    lib().ostaple_autotune(2 + int(candidate))
+
+
 def autotune_report() -> str:
     """One line per tuned (kernel, lattice, variant): the chosen candidate and
     each candidate's microseconds per launch."""

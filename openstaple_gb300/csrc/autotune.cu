@@ -31,9 +31,8 @@ int g_forced = -1;    // >= 0: every tuned launch uses this candidate (tests)
 const char* kernel_name(int k) {
   switch (k) {
     case TUNE_MX_DOE:
-      return "k_mx_doe (threads per block, hops in flight; s = all eight staged by cp.async) "
-             "{128/1, 256/1, 64/1, 128/2, 128/4, 256/2, 64/2, 128/s, 256/s}";
-    case TUNE_MX_DEO: return "k_mx_deo_dot hops in flight {1, 2, 4, s (all eight staged by cp.async)}";
+      return "k_mx_doe (threads per block, hops in flight) {128/1, 256/1, 64/1, 128/2, 128/4, 256/2, 64/2}";
+    case TUNE_MX_DEO: return "k_mx_deo_dot hops in flight {1, 2, 4}";
     case TUNE_B_DOE: return "k_b_doe systems per thread {default, 1, 2, 4}";
     default: return "k_cgm_doe systems per thread {default, 1, 2, 4}";
   }

@@ -466,94 +466,4 @@ OST_D void hop_fb(const Geom& g, const LV& u, const float2* in, const void* phas
   for (int c = 0; c < 3; ++c) aux[c] = cadd(accb[c], accf[c]);
 }
 
-// ---- staged hops (16-bit links, sign bytes) ----
-// Every load of the eight hops of a site is in flight at once: the links
-// (16 + 8 bytes) and the input vectors (3 x 8 bytes) go to shared memory by
-// cp.async, which holds no registers while the copies are outstanding, and
-// the sign bytes by plain loads.  Shared memory per block of T threads:
-// [8][T] uint4, [8][T] uint2, [24][T] float2 (384 B per thread), each
-// thread using only its own column, so no block barrier is needed: the
-// copies of a thread are visible to it after its cp.async.wait_group.  The
-// arithmetic is hop_fb's, in the same order, so the results are the same
-// bits.
-constexpr int STAGE_BYTES_PER_THREAD = 8 * 16 + 8 * 8 + 24 * 8;
-
-OST_D unsigned smem_addr(const void* p) { return unsigned(__cvta_generic_to_shared(p)); }
-OST_D void cp_async16(void* dst, const void* src) {
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
-}
-OST_D void cp_async8(void* dst, const void* src) {
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
-}
-OST_D void cp_async8_keep(void* dst, const void* src, unsigned long long pol) {
-  asm volatile("cp.async.ca.shared.global.L2::cache_hint [%0], [%1], 8, %2;" ::"r"(smem_addr(dst)), "l"(src), "l"(pol)
-               : "memory");
-}
-OST_D void cp_async_wait_all() { asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory"); }
-
-struct HopStage {
-  uint4* a;     // [8][T]
-  uint2* b;     // [8][T]
-  float2* v;    // [24][T]
-  int T, t;
-  OST_D HopStage(unsigned char* smem, int T_, int t_)
-      : a(reinterpret_cast<uint4*>(smem)), b(reinterpret_cast<uint2*>(smem + 8 * 16 * T_)),
-        v(reinterpret_cast<float2*>(smem + 8 * 24 * T_)), T(T_), t(t_) {}
-};
-
-// site, neighbours, the eight links' copies and sign bytes (the links and
-// signs are never written by the solve: issued before pdl_wait)
-template <int P>
-OST_D void stage_links(const Geom& g, const LinkQ16& u, const unsigned char* sg, int idx, int fwd[4], int bwd[4],
-                       unsigned char sb[8], const HopStage& st) {
-  const long sh = g.sizeh;
-  Site s = site_of(g, idx, P);
-  neighbours(g, s, fwd, bwd);
-#pragma unroll
-  for (int hm = 0; hm < 8; ++hm) {
-    const bool back = hm < 4;
-    const int mu = hm & 3;
-    const int dir = back ? 2 * mu + (1 - P) : 2 * mu + P;
-    const int l = back ? bwd[mu] : idx;
-    cp_async16(st.a + hm * st.T + st.t, u.a + long(dir) * sh + l);
-    cp_async8(st.b + hm * st.T + st.t, u.b + long(dir) * sh + l);
-    sb[hm] = __ldg(sg + long(dir) * sh + l);
-  }
-}
-
-OST_D void stage_vectors(const float2* in, long sh, int idx, const int fwd[4], const int bwd[4], const HopStage& st) {
-  const unsigned long long pol = l2_keep_policy();
-#pragma unroll
-  for (int hm = 0; hm < 8; ++hm) {
-    const int mu = hm & 3;
-    const int j = hm < 4 ? bwd[mu] : fwd[mu];
-#pragma unroll
-    for (int c = 0; c < 3; ++c) cp_async8_keep(st.v + (hm * 3 + c) * st.T + st.t, in + c * sh + j, pol);
-  }
-}
-
-// the hop term from the staged copies (after cp_async_wait_all)
-OST_D void hop_fb_staged(const unsigned char sb[8], const HopStage& st, float2 aux[3]) {
-  float2 accb[3], accf[3];
-#pragma unroll
-  for (int c = 0; c < 3; ++c) accb[c] = accf[c] = make_float2(0.f, 0.f);
-#pragma unroll
-  for (int hm = 0; hm < 8; ++hm) {
-    const bool back = hm < 4;
-    float2 v[3];
-#pragma unroll
-    for (int c = 0; c < 3; ++c) v[c] = st.v[(hm * 3 + c) * st.T + st.t];
-    LinkRaw<LinkQ16> raw;
-    raw.a = st.a[hm * st.T + st.t];
-    raw.b = st.b[hm * st.T + st.t];
-    apply_hop_phase<PH_SIGN8>(v, back, 0.f, sb[hm]);
-    float2 m[6];
-    raw.rows(m);
-    if (back) mac_hop(accb, m, v, true);
-    else mac_hop(accf, m, v, false);
-  }
-#pragma unroll
-  for (int c = 0; c < 3; ++c) aux[c] = cadd(accb[c], accf[c]);
-}
-
 }  // namespace ost

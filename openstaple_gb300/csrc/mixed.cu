@@ -154,70 +154,6 @@ k_mx_deo_dot(Geom g, LV u, const void* __restrict__ ph, const float2* __restrict
   }
 }
 
-// Staged variants of the two hops (16-bit links and sign bytes only): all
-// loads of a site's eight hops in flight at once through cp.async
-// (dslash.cuh), links and signs issued before the programmatic wait.  Same
-// arithmetic as k_mx_doe / k_mx_deo_dot: the same bits.
-__global__ void __launch_bounds__(256)
-k_mx_doe_st(Geom g, LinkQ16 u, const void* __restrict__ ph, const float2* __restrict__ p, float2* __restrict__ t,
-            const MixScal* sc) {
-  extern __shared__ __align__(16) unsigned char stage_smem[];
-  if (halted(sc)) return;
-  const HopStage st(stage_smem, blockDim.x, threadIdx.x);
-  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  const bool live = idx < g.sizeh;
-  int fwd[4], bwd[4];
-  unsigned char sb[8];
-  if (live) stage_links<1>(g, u, static_cast<const unsigned char*>(ph), idx, fwd, bwd, sb, st);
-  pdl_wait();               // p from k_mx_pupdate
-  pdl_trigger();
-  if (live) stage_vectors(p, g.sizeh, idx, fwd, bwd, st);
-  cp_async_wait_all();
-  if (!live) return;
-  float2 aux[3];
-  hop_fb_staged(sb, st, aux);
-  const unsigned long long pol = l2_keep_policy();
-#pragma unroll
-  for (int c = 0; c < 3; ++c) st_keep2(t + c * long(g.sizeh) + idx, make_float2(0.5f * aux[c].x, 0.5f * aux[c].y), pol);
-}
-
-__global__ void __launch_bounds__(MX_THREADS)
-k_mx_deo_dot_st(Geom g, LinkQ16 u, const void* __restrict__ ph, const float2* __restrict__ t,
-                const float2* __restrict__ p, float2* __restrict__ s, MixScal* sc, ReduceWs ws) {
-  extern __shared__ __align__(16) unsigned char stage_smem[];
-  if (halted(sc)) return;
-  const HopStage st(stage_smem, blockDim.x, threadIdx.x);
-  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  const bool live = idx < g.sizeh;
-  int fwd[4], bwd[4];
-  unsigned char sb[8];
-  if (live) stage_links<0>(g, u, static_cast<const unsigned char*>(ph), idx, fwd, bwd, sb, st);
-  pdl_wait();               // t from k_mx_doe
-  pdl_trigger();
-  if (live) stage_vectors(t, g.sizeh, idx, fwd, bwd, st);
-  cp_async_wait_all();
-  float v[1] = {0.0f};
-  if (live) {
-    const float m2 = float(sc->m2);
-    float2 aux[3];
-    hop_fb_staged(sb, st, aux);
-    const unsigned long long pol = l2_keep_policy();
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      const long k = c * long(g.sizeh) + idx;
-      float2 pv = ldg_keep(p + k, pol);
-      float2 r = make_float2(fmaf(pv.x, m2, -0.5f * aux[c].x), fmaf(pv.y, m2, -0.5f * aux[c].y));
-      st_keep2(s + k, r, pol);
-      v[0] = fmaf(pv.x, r.x, fmaf(pv.y, r.y, v[0]));
-    }
-  }
-  double tot[1];
-  if (grid_reduce_f32w<1>(v, ws, tot)) {
-    sc->pAp = tot[0];
-    sc->alpha = sc->delta / tot[0];
-  }
-}
-
 // x_f += alpha p ; unless a reliable update is due: r -= alpha s, lambda = |r|^2,
 // beta = lambda / delta, delta = lambda.
 __global__ void k_mx_update(float4* __restrict__ xf, float4* __restrict__ r, const float4* __restrict__ p,
@@ -402,34 +338,15 @@ void fp64_mdagm(const MixedBuffers& B, double2* out, const double2* in, double2*
 }
 
 // Launch shapes the autotuner tries (the first is the default): block size
-// and hops in flight, hb = STAGED for the cp.async variants (16-bit links
-// with sign bytes; with other link formats the default shape runs instead).
-// The block size of k_mx_deo_dot fixes the summation order of <p, Ap>, so
-// only its hops in flight are tuned.
+// and hops in flight.  The block size of k_mx_deo_dot fixes the summation
+// order of <p, Ap>, so only its hops in flight are tuned.
 struct HopShape {
   int threads, hb;
 };
-constexpr int STAGED = 8;
-constexpr int N_DOE_SHAPES = 9, N_DEO_SHAPES = 4;
+constexpr int N_DOE_SHAPES = 7, N_DEO_SHAPES = 3;
 static const HopShape kDoeShapes[N_DOE_SHAPES] = {{MX_THREADS, 1}, {256, 1}, {64, 1}, {MX_THREADS, 2},
-                                                  {MX_THREADS, 4}, {256, 2}, {64, 2}, {MX_THREADS, STAGED},
-                                                  {256, STAGED}};
-static const HopShape kDeoShapes[N_DEO_SHAPES] = {{MX_THREADS, 1}, {MX_THREADS, 2}, {MX_THREADS, 4},
-                                                  {MX_THREADS, STAGED}};
-
-// The staged kernels' dynamic shared memory plus the reduction's static
-// shared memory exceed the 48 KB a kernel gets without opting in.
-template <typename K>
-void allow_stage_smem(K kernel, int threads) {
-  static int granted = 0;
-  const int bytes = threads * STAGE_BYTES_PER_THREAD;
-  if (bytes > granted) {
-    OST_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-    granted = bytes;
-  }
-}
-
-bool stageable(const MixedBuffers& B) { return B.q16 && B.ph32_mode == PH_SIGN8; }
+                                                  {MX_THREADS, 4}, {256, 2}, {64, 2}};
+static const HopShape kDeoShapes[N_DEO_SHAPES] = {{MX_THREADS, 1}, {MX_THREADS, 2}, {MX_THREADS, 4}};
 
 // Calls f with the view of the sloppy links the FP32 iteration reads.
 template <typename F>
@@ -451,17 +368,6 @@ void launch_mx_doe_t(int threads, const MixedBuffers& B, const MixScal* sc, cuda
 }
 
 void launch_mx_doe(HopShape sh, const MixedBuffers& B, const MixScal* sc, cudaStream_t st) {
-  if (sh.hb == STAGED) {
-    if (!stageable(B)) {
-      launch_mx_doe_t<1>(MX_THREADS, B, sc, st);
-      return;
-    }
-    const Geom& g = rt().g;
-    allow_stage_smem(k_mx_doe_st, sh.threads);
-    launch_pdl_smem(k_mx_doe_st, blocks_for(g.sizeh, sh.threads), sh.threads,
-                    size_t(sh.threads) * STAGE_BYTES_PER_THREAD, st, g, B.uq, B.ph32, B.p, B.t, sc);
-    return;
-  }
   if (sh.hb == 4) launch_mx_doe_t<4>(sh.threads, B, sc, st);
   else if (sh.hb == 2) launch_mx_doe_t<2>(sh.threads, B, sc, st);
   else launch_mx_doe_t<1>(sh.threads, B, sc, st);
@@ -480,17 +386,6 @@ void launch_mx_deo_dot_t(const MixedBuffers& B, MixScal* sc, ReduceWs ws, cudaSt
 }
 
 void launch_mx_deo_dot(HopShape sh, const MixedBuffers& B, MixScal* sc, ReduceWs ws, cudaStream_t st) {
-  if (sh.hb == STAGED) {
-    if (!stageable(B)) {
-      launch_mx_deo_dot_t<1>(B, sc, ws, st);
-      return;
-    }
-    const Geom& g = rt().g;
-    allow_stage_smem(k_mx_deo_dot_st, MX_THREADS);
-    launch_pdl_smem(k_mx_deo_dot_st, blocks_for(g.sizeh, MX_THREADS), MX_THREADS,
-                    size_t(MX_THREADS) * STAGE_BYTES_PER_THREAD, st, g, B.uq, B.ph32, B.t, B.p, B.s, sc, ws);
-    return;
-  }
   if (sh.hb == 4) launch_mx_deo_dot_t<4>(B, sc, ws, st);
   else if (sh.hb == 2) launch_mx_deo_dot_t<2>(B, sc, ws, st);
   else launch_mx_deo_dot_t<1>(B, sc, ws, st);

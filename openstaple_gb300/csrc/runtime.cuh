@@ -68,21 +68,6 @@ bool pdl_enabled();
 bool device_loop_enabled();
 
 template <typename... P, typename... A>
-void launch_pdl_smem(void (*kernel)(P...), int grid, int block, size_t smem, cudaStream_t st, A&&... args) {
-  cudaLaunchConfig_t cfg{};
-  cfg.gridDim = dim3(unsigned(grid));
-  cfg.blockDim = dim3(unsigned(block));
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = st;
-  cudaLaunchAttribute at[1];
-  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  at[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = at;
-  cfg.numAttrs = pdl_enabled() ? 1 : 0;
-  OST_CUDA(cudaLaunchKernelEx(&cfg, kernel, static_cast<P>(args)...));
-}
-
-template <typename... P, typename... A>
 void launch_pdl(void (*kernel)(P...), int grid, int block, cudaStream_t st, A&&... args) {
   cudaLaunchConfig_t cfg{};
   cfg.gridDim = dim3(unsigned(grid));

@@ -75,8 +75,8 @@ def test_every_shape_gives_the_same_bits(lat):
         lat.present(a)
     api.autotune(False)
     base = _solve_all(lat, u, ph, b)
-    for cand in (1, 2, 3, 4, 5, 6, 7, 8):
-        api.autotune(2 + cand)
+    for cand in (1, 2, 3, 4, 5, 6):
+        api.autotune_force(cand)
         got = _solve_all(lat, u, ph, b)
         for k, (g, r) in enumerate(zip(got, base)):
             assert np.array_equal(g.view(np.uint64), r.view(np.uint64)), (cand, k)
