@@ -12,6 +12,7 @@
 #include <cmath>
 #include <cstring>
 #include <type_traits>
+#include <vector>
 #include "autotune.cuh"
 #include "dslash.cuh"
 #include "kernels.cuh"
@@ -483,11 +484,18 @@ void enqueue_reliable_update(const MixedBuffers& B, double m2, MixScal* sc, cuda
   OST_LAUNCH_CHECK();
 }
 
-template <typename F>
-bool capture_into(cudaStream_t cs, cudaGraph_t* g, F&& f) {
-  if (cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return false;
-  f();
-  return cudaStreamEndCapture(cs, g) == cudaSuccess && *g;
+// the nodes of g that no other node depends on
+std::vector<cudaGraphNode_t> leaf_nodes(cudaGraph_t g) {
+  size_t n = 0;
+  std::vector<cudaGraphNode_t> leaves;
+  if (cudaGraphGetNodes(g, nullptr, &n) != cudaSuccess || n == 0) return leaves;
+  std::vector<cudaGraphNode_t> nodes(n);
+  if (cudaGraphGetNodes(g, nodes.data(), &n) != cudaSuccess) return leaves;
+  for (cudaGraphNode_t v : nodes) {
+    size_t d = 0;
+    if (cudaGraphNodeGetDependentNodes(v, nullptr, nullptr, &d) == cudaSuccess && d == 0) leaves.push_back(v);
+  }
+  return leaves;
 }
 
 struct LoopCache {
@@ -516,17 +524,14 @@ cudaGraphExec_t device_loop(const MixedBuffers& B, const MixedOptions& o, MixSca
   if (g_loop.exec) cudaGraphExecDestroy(g_loop.exec);
   g_loop.exec = nullptr;
   const unsigned long long counted = g_kernel_launches;   // building launches nothing
-  cudaGraph_t graph = nullptr, chunk_g = nullptr, rel_g = nullptr, test_g = nullptr;
+  // graph: while (h_loop) { chunk of iterations; k_mx_rel_test;
+  //                         if (h_rel) { reliable update }; k_mx_loop_test }
+  // Both condition-setting kernels sit directly in the while body.
+  cudaGraph_t graph = nullptr;
   cudaGraphConditionalHandle h_loop{}, h_rel{};
   bool ok = cudaGraphCreate(&graph, 0) == cudaSuccess;
   ok = ok && cudaGraphConditionalHandleCreate(&h_loop, graph, 1, cudaGraphCondAssignDefault) == cudaSuccess;
   ok = ok && cudaGraphConditionalHandleCreate(&h_rel, graph, 0, cudaGraphCondAssignDefault) == cudaSuccess;
-  ok = ok && capture_into(cs, &chunk_g, [&] {
-    for (int k = 0; k < o.chunk; ++k) enqueue_iteration(B, sc, cs);
-    k_mx_rel_test<<<1, 1, 0, cs>>>(h_rel, sc);
-  });
-  ok = ok && capture_into(cs, &rel_g, [&] { enqueue_reliable_update(B, o.mass2, sc, cs); });
-  ok = ok && capture_into(cs, &test_g, [&] { k_mx_loop_test<<<1, 1, 0, cs>>>(h_loop, sc, trips, max_trips); });
   cudaGraphNodeParams wp{};
   cudaGraphNode_t wnode;
   if (ok) {
@@ -536,23 +541,53 @@ cudaGraphExec_t device_loop(const MixedBuffers& B, const MixedOptions& o, MixSca
     wp.conditional.size = 1;
     ok = cudaGraphAddNode(&wnode, graph, nullptr, nullptr, 0, &wp) == cudaSuccess;
   }
+  cudaGraph_t body = ok ? wp.conditional.phGraph_out[0] : nullptr;
+  // the chunk and the reliable-update test, captured into the body
   if (ok) {
-    cudaGraph_t body = wp.conditional.phGraph_out[0];
-    cudaGraphNode_t n1, n2, n3, n4;
-    cudaGraphNodeParams ip{};
+    ok = cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) ==
+         cudaSuccess;
+    if (ok) {
+      for (int k = 0; k < o.chunk; ++k) enqueue_iteration(B, sc, cs);
+      k_mx_rel_test<<<1, 1, 0, cs>>>(h_rel, sc);
+      ok = cudaStreamEndCapture(cs, &body) == cudaSuccess;
+    }
+  }
+  std::vector<cudaGraphNode_t> leaves = ok ? leaf_nodes(body) : std::vector<cudaGraphNode_t>{};
+  ok = ok && leaves.size() == 1;
+  cudaGraphNodeParams ip{};
+  cudaGraphNode_t inode, tnode;
+  if (ok) {
     ip.type = cudaGraphNodeTypeConditional;
     ip.conditional.handle = h_rel;
     ip.conditional.type = cudaGraphCondTypeIf;
     ip.conditional.size = 1;
-    ok = cudaGraphAddChildGraphNode(&n1, body, nullptr, 0, chunk_g) == cudaSuccess;
-    ok = ok && cudaGraphAddNode(&n2, body, &n1, nullptr, 1, &ip) == cudaSuccess;
-    ok = ok && cudaGraphAddChildGraphNode(&n4, ip.conditional.phGraph_out[0], nullptr, 0, rel_g) == cudaSuccess;
-    ok = ok && cudaGraphAddChildGraphNode(&n3, body, &n2, 1, test_g) == cudaSuccess;
+    ok = cudaGraphAddNode(&inode, body, leaves.data(), nullptr, 1, &ip) == cudaSuccess;
+  }
+  if (ok) {   // the reliable update, captured into the if body
+    cudaGraph_t ibody = ip.conditional.phGraph_out[0];
+    ok = cudaStreamBeginCaptureToGraph(cs, ibody, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) ==
+         cudaSuccess;
+    if (ok) {
+      enqueue_reliable_update(B, o.mass2, sc, cs);
+      ok = cudaStreamEndCapture(cs, &ibody) == cudaSuccess;
+    }
+  }
+  if (ok) {   // the loop test after the if node
+    const MixScal* csc = sc;
+    int mt = max_trips;
+    void* args[] = {&h_loop, &csc, &trips, &mt};
+    cudaKernelNodeParams kp{};
+    kp.func = reinterpret_cast<void*>(k_mx_loop_test);
+    kp.gridDim = dim3(1);
+    kp.blockDim = dim3(1);
+    kp.sharedMemBytes = 0;
+    kp.kernelParams = args;
+    kp.extra = nullptr;
+    ok = cudaGraphAddKernelNode(&tnode, body, &inode, 1, &kp) == cudaSuccess;
   }
   cudaGraphExec_t exec = nullptr;
   if (ok) ok = cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess;
-  for (cudaGraph_t gph : {chunk_g, rel_g, test_g, graph})
-    if (gph) cudaGraphDestroy(gph);
+  if (graph) cudaGraphDestroy(graph);
   g_kernel_launches = counted;
   if (!ok) {
     if (exec) cudaGraphExecDestroy(exec);
