@@ -119,6 +119,16 @@ OST_D void hop_multi(const Geom& g, const LV& u, const float2* in, long vs, cons
   }
 }
 
+// Launched early (programmatic dependent launch): the first lane of each
+// site fetches the links of its eight hops into L2 while the previous kernel
+// finishes (no kernel of the solve writes the links).
+template <int LANES, int P, typename LV>
+OST_D void prefetch_site_links(const Geom& g, const LV& u) {
+  const long tid = long(blockIdx.x) * BT + threadIdx.x;
+  const long site = tid / LANES;
+  if (tid % LANES == 0 && site < g.sizeh) prefetch_links<P>(g, u, int(site));
+}
+
 // thread -> (site, first system slot of its lane); slots beyond NS read a
 // valid system (slot 0) and discard the result.  Returns idx < sizeh.
 template <int NS, int SPL_ = 0>
@@ -144,6 +154,7 @@ k_b_doe(Geom g, LV u, const void* __restrict__ ph, const float2* __restrict__ p,
         const BatchScal* sc) {
   typedef HopLayout<NS, SPL_> H;
   if (!active_mask(sc)) return;   // flags of k_b_update, two launches back
+  prefetch_site_links<H::LANES, 1>(g, u);
   pdl_wait();                     // p from k_b_pupdate
   pdl_trigger();
   int idx, sys[H::SPL];
@@ -200,6 +211,7 @@ k_b_deo_dot(Geom g, LV u, const void* __restrict__ ph, const float2* __restrict_
             float2* __restrict__ s, long vs, BatchScal* sc, ReduceWs ws) {
   typedef HopLayout<NS> H;
   if (!active_mask(sc)) return;
+  prefetch_site_links<H::LANES, 0>(g, u);
   pdl_wait();                     // t from k_b_doe
   pdl_trigger();
   int idx, sys[H::SPL];
