@@ -152,6 +152,8 @@ def parse_args():
     ap.add_argument("--therm-nometro", type=int, default=20,
                     help="of which the first ones skip the Metropolis test (the reference's ThermNtraj)")
     ap.add_argument("--stout", type=int, default=2, help="stout steps of rho = 0.15 on the thermalised links")
+    ap.add_argument("--no-link-cache", action="store_true",
+                    help="always generate the thermalised configuration (no ILDG cache file is read or written)")
     return ap.parse_args()
 
 
@@ -242,7 +244,7 @@ def thermalized_links(lat, dims, seed, args):
     from openstaple_gb300 import api, fields as F
     from openstaple_gb300.native import act_params
     n0 = min(args.therm_nometro, args.therm)
-    u, info = cached_links(lat, dims, seed, args, n0)
+    u, info = (None, None) if args.no_link_cache else cached_links(lat, dims, seed, args, n0)
     if u is None:
         u = F.cold_links(dims)
         lat.present(u)
@@ -263,7 +265,8 @@ def thermalized_links(lat, dims, seed, args):
                 "integrator": "2MN, 18 steps x 4 gauge substeps, length 1, FP32 molecular dynamics, FP64 Metropolis",
                 "seed": seed}
         lat.update_host(u)
-        store_links(u, dims, seed, args, n0, info)
+        if not args.no_link_cache:
+            store_links(u, dims, seed, args, n0, info)
     info = dict(info, stout={"steps": args.stout, "rho": 0.15})
     if args.stout > 0:
         api.set_stout_rho(0.15)

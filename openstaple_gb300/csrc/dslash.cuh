@@ -320,45 +320,6 @@ OST_D void apply_hop_phase(float2 v[3], bool back, float arg, unsigned char sb) 
   }
 }
 
-// L2 residency of the FP32 iteration's vectors.  At 32^4 the five vectors of
-// the mixed solver's FP32 iteration (p, t, s, r, x: 63 MB) fit in the 126 MB
-// L2, but each hop kernel streams 105 MB of links and sign bytes through it
-// and pushes them out between the kernels of an iteration.  The vector loads
-// and stores of the iteration therefore carry an evict-last L2 policy, the
-// links keep their evict-first (streaming) loads.
-OST_D unsigned long long l2_keep_policy() {
-  unsigned long long pol;
-  asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
-  return pol;
-}
-OST_D float2 ldg_keep(const float2* a, unsigned long long pol) {
-  float2 v;
-  asm("ld.global.nc.L2::cache_hint.v2.f32 {%0, %1}, [%2], %3;" : "=f"(v.x), "=f"(v.y) : "l"(a), "l"(pol));
-  return v;
-}
-// loads of data the same thread stores again later: ordered by volatile
-OST_D float4 ld_keep4(const float4* a, unsigned long long pol) {
-  float4 v;
-  asm volatile("ld.global.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
-               : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "l"(a), "l"(pol) : "memory");
-  return v;
-}
-OST_D float2 ld_keep2(const float2* a, unsigned long long pol) {
-  float2 v;
-  asm volatile("ld.global.L2::cache_hint.v2.f32 {%0, %1}, [%2], %3;" : "=f"(v.x), "=f"(v.y) : "l"(a), "l"(pol)
-               : "memory");
-  return v;
-}
-OST_D void st_keep2(float2* a, float2 v, unsigned long long pol) {
-  asm volatile("st.global.L2::cache_hint.v2.f32 [%0], {%1, %2}, %3;" ::"l"(a), "f"(v.x), "f"(v.y), "l"(pol)
-               : "memory");
-}
-OST_D void st_keep4(float4* a, float4 v, unsigned long long pol) {
-  asm volatile("st.global.L2::cache_hint.v4.f32 [%0], {%1, %2, %3, %4}, %5;" ::"l"(a), "f"(v.x), "f"(v.y), "f"(v.z),
-               "f"(v.w), "l"(pol)
-               : "memory");
-}
-
 // acc += W v with W = U (forward) or U^+ (backward), U rebuilt from rows m
 OST_D void mac_hop(float2 acc[3], const float2 m[6], const float2 v[3], bool back) {
   const float2 r20 = conj_cross(m[1], m[5], m[2], m[4]);
@@ -395,11 +356,7 @@ OST_D void hop4(const LV& u, const float2* in, const void* phases, long sh, int 
       const int j = back ? bwd[mu] : fwd[mu];   // input site
       const int l = back ? j : idx;             // link site
       raw[k].load(u, dir, l);
-      {
-        const unsigned long long pol = l2_keep_policy();
-#pragma unroll
-        for (int c = 0; c < 3; ++c) v[k][c] = ldg_keep(in + c * sh + j, pol);
-      }
+      load_vec(in, sh, j, v[k]);
       arg[k] = 0.f;
       sb[k] = 0;
       if (PH == PH_ANGLE) arg[k] = __ldcs(static_cast<const float*>(phases) + long(dir) * sh + l);

@@ -118,9 +118,8 @@ k_mx_doe(Geom g, LV u, const void* __restrict__ ph, const float2* __restrict__ p
   if (idx >= g.sizeh) return;
   float2 aux[3];
   hop_fb<1, PH, LV, HB>(g, u, p, ph, idx, aux);
-  const unsigned long long pol = l2_keep_policy();
 #pragma unroll
-  for (int c = 0; c < 3; ++c) st_keep2(t + c * long(g.sizeh) + idx, make_float2(0.5f * aux[c].x, 0.5f * aux[c].y), pol);
+  for (int c = 0; c < 3; ++c) t[c * long(g.sizeh) + idx] = make_float2(0.5f * aux[c].x, 0.5f * aux[c].y);
 }
 
 // s = m2 p - D_eo t ; pAp = Re<p, s> ; alpha = delta / pAp
@@ -138,13 +137,12 @@ k_mx_deo_dot(Geom g, LV u, const void* __restrict__ ph, const float2* __restrict
     const float m2 = float(sc->m2);
     float2 aux[3];
     hop_fb<0, PH, LV, HB>(g, u, t, ph, idx, aux);
-    const unsigned long long pol = l2_keep_policy();
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       const long k = c * long(g.sizeh) + idx;
-      float2 pv = ldg_keep(p + k, pol);
+      float2 pv = p[k];
       float2 r = make_float2(fmaf(pv.x, m2, -0.5f * aux[c].x), fmaf(pv.y, m2, -0.5f * aux[c].y));
-      st_keep2(s + k, r, pol);
+      s[k] = r;
       v[0] = fmaf(pv.x, r.x, fmaf(pv.y, r.y, v[0]));
     }
   }
@@ -175,32 +173,27 @@ __global__ void k_mx_update(float4* __restrict__ xf, float4* __restrict__ r, con
   const double lm = sc->last_max > delta ? sc->last_max : delta;
   const bool rel = sc->every > 0 ? ((sc->iter + 1) % sc->every == 0) : (delta < sc->frac * lm);
   const float a = float(sc->alpha);
-  const unsigned long long pol = l2_keep_policy();
   float v[1] = {0.0f};
   // two elements per pass, all loads issued before use
   for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n4; i += 2 * stride) {
     const long j = i + stride;
     const bool two = j < n4;
-    float4 pv0 = ld_keep4(p + i, pol), xv0 = ld_keep4(xf + i, pol), pv1, xv1, sv0, rv0, sv1, rv1;
-    if (two) { pv1 = ld_keep4(p + j, pol); xv1 = ld_keep4(xf + j, pol); }
-    if (!rel) {
-      sv0 = ld_keep4(s + i, pol);
-      rv0 = ld_keep4(r + i, pol);
-      if (two) { sv1 = ld_keep4(s + j, pol); rv1 = ld_keep4(r + j, pol); }
-    }
+    float4 pv0 = p[i], xv0 = xf[i], pv1, xv1, sv0, rv0, sv1, rv1;
+    if (two) { pv1 = p[j]; xv1 = xf[j]; }
+    if (!rel) { sv0 = s[i]; rv0 = r[i]; if (two) { sv1 = s[j]; rv1 = r[j]; } }
     xv0.x = fmaf(a, pv0.x, xv0.x); xv0.y = fmaf(a, pv0.y, xv0.y); xv0.z = fmaf(a, pv0.z, xv0.z); xv0.w = fmaf(a, pv0.w, xv0.w);
-    st_keep4(xf + i, xv0, pol);
+    xf[i] = xv0;
     if (two) {
       xv1.x = fmaf(a, pv1.x, xv1.x); xv1.y = fmaf(a, pv1.y, xv1.y); xv1.z = fmaf(a, pv1.z, xv1.z); xv1.w = fmaf(a, pv1.w, xv1.w);
-      st_keep4(xf + j, xv1, pol);
+      xf[j] = xv1;
     }
     if (!rel) {
       rv0.x = fmaf(-a, sv0.x, rv0.x); rv0.y = fmaf(-a, sv0.y, rv0.y); rv0.z = fmaf(-a, sv0.z, rv0.z); rv0.w = fmaf(-a, sv0.w, rv0.w);
-      st_keep4(r + i, rv0, pol);
+      r[i] = rv0;
       v[0] = fmaf(rv0.x, rv0.x, fmaf(rv0.y, rv0.y, fmaf(rv0.z, rv0.z, fmaf(rv0.w, rv0.w, v[0]))));
       if (two) {
         rv1.x = fmaf(-a, sv1.x, rv1.x); rv1.y = fmaf(-a, sv1.y, rv1.y); rv1.z = fmaf(-a, sv1.z, rv1.z); rv1.w = fmaf(-a, sv1.w, rv1.w);
-        st_keep4(r + j, rv1, pol);
+        r[j] = rv1;
         v[0] = fmaf(rv1.x, rv1.x, fmaf(rv1.y, rv1.y, fmaf(rv1.z, rv1.z, fmaf(rv1.w, rv1.w, v[0]))));
       }
     }
@@ -230,15 +223,12 @@ __global__ void k_mx_pupdate(float4* __restrict__ p, const float4* __restrict__ 
   if (guarded && halted(sc)) return;
   pdl_trigger();
   const float b = float(sc->beta);
-  const unsigned long long pol = l2_keep_policy();
   for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n4; i += 2 * stride) {
     const long j = i + stride;
-    float4 pv = ld_keep4(p + i, pol), rv = ld_keep4(r + i, pol), pw, rw;
-    if (j < n4) { pw = ld_keep4(p + j, pol); rw = ld_keep4(r + j, pol); }
-    st_keep4(p + i, make_float4(fmaf(b, pv.x, rv.x), fmaf(b, pv.y, rv.y), fmaf(b, pv.z, rv.z), fmaf(b, pv.w, rv.w)), pol);
-    if (j < n4)
-      st_keep4(p + j, make_float4(fmaf(b, pw.x, rw.x), fmaf(b, pw.y, rw.y), fmaf(b, pw.z, rw.z), fmaf(b, pw.w, rw.w)),
-               pol);
+    float4 pv = p[i], rv = r[i], pw, rw;
+    if (j < n4) { pw = p[j]; rw = r[j]; }
+    p[i] = make_float4(fmaf(b, pv.x, rv.x), fmaf(b, pv.y, rv.y), fmaf(b, pv.z, rv.z), fmaf(b, pv.w, rv.w));
+    if (j < n4) p[j] = make_float4(fmaf(b, pw.x, rw.x), fmaf(b, pw.y, rw.y), fmaf(b, pw.z, rw.z), fmaf(b, pw.w, rw.w));
   }
 }
 
