@@ -248,13 +248,10 @@ __global__ void __launch_bounds__(H_THREADS)
 k_gauge_force(Geom g, const C* __restrict__ u, int rows, int parts, int mode, C* stap,
               decltype(C().x)* alg, double fact) {
   typedef decltype(C().x) Rt;
-  // block b takes direction b % 8 of the sites of block b / 8: the eight
-  // directions of a range of sites run side by side, so the staple walks of
-  // concurrent blocks share the neighbouring links in L2 (direction after
-  // direction, every pass re-read the whole link field from DRAM)
-  const int dir = int(blockIdx.x % 8);
-  const long x = (blockIdx.x / 8) * long(blockDim.x) + threadIdx.x;
-  if (x >= g.sizeh) return;
+  const long t = blockIdx.x * long(blockDim.x) + threadIdx.x;
+  if (t >= 8L * g.sizeh) return;
+  const int dir = int(t / g.sizeh);
+  const long x = t - long(dir) * g.sizeh;
   const int mu = dir >> 1, p = dir & 1;
   const Site s = site_of(g, int(x), p);
   Walker<C> w{g, u, rows, pos_of(s), p};
@@ -299,8 +296,8 @@ template <typename R>
 void launch_gauge_force(HmcLinks<R> u, int parts, int mode, typename cplx_t<R>::type* stap, R* alg, double fact,
                         cudaStream_t st) {
   const Geom& g = rt().g;
-  const int grid = int(8 * ((g.sizeh + H_THREADS - 1) / H_THREADS));
-  k_gauge_force<typename cplx_t<R>::type><<<grid, H_THREADS, 0, st>>>(g, u.p, u.rows, parts, mode, stap, alg, fact);
+  k_gauge_force<typename cplx_t<R>::type><<<links_grid(g.sizeh), H_THREADS, 0, st>>>(g, u.p, u.rows, parts, mode,
+                                                                                       stap, alg, fact);
   OST_LAUNCH_CHECK();
 }
 
