@@ -617,7 +617,7 @@ def main():
             lat.present(a, copy=False)
         h2d = ue.nbytes + phe.nbytes + be.nbytes + xe.nbytes
         d2h = xe.nbytes
-        times, phases = [], []
+        times, phases, copies, reads = [], [], [], []
         e2e_steps = max(args.steps, 9)   # enough steps for a median that host stalls do not move
         for k in range(args.warmup + e2e_steps):
             xe[...] = 0
@@ -625,6 +625,7 @@ def main():
             t0 = time.perf_counter()
             for a in (ue, phe, be, xe):
                 lat.update_device(a)
+            tc = time.perf_counter()
             c0 = torch.cuda.Event(enable_timing=True)
             c0.record(stream)
             if args.solver == "learned":
@@ -635,10 +636,13 @@ def main():
                 api.invert_mixed(ue, phe, args.mass, 0.0, xe, be, args.res, 100000, args.every, args.delta)
             c1 = torch.cuda.Event(enable_timing=True)
             c1.record(stream)
+            tr = time.perf_counter()
             lat.update_host(xe)
             dt = time.perf_counter() - t0
             if k >= args.warmup:
                 times.append(dt)
+                copies.append(round(1e3 * (tc - t0), 3))
+                reads.append(round(1e3 * (t0 + dt - tr), 3))
                 # device time of the solve call alone (from after the copies
                 # to before the read-back), to tell host stalls from GPU work
                 phases.append(round(c0.elapsed_time(c1), 3))
@@ -652,6 +656,7 @@ def main():
         e2e = {"value": world * nrhs * 1e3 / e2e_ms, "unit": "solves/s", "ms_per_step": e2e_ms,
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                "step_ms": [round(1e3 * t, 3) for t in times], "solve_device_ms": phases,
+               "h2d_host_ms": copies, "d2h_host_ms": reads,
                "statistic": "median of the timed steps",
                "host_buffers": "page-locked (torch pin_memory)"}
 
