@@ -1,4 +1,5 @@
 // capi_batched.cu -- C entry points of the batched solvers.
+#include <cstdlib>
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -251,12 +252,21 @@ int ostaple_multishift_batch(const su3_soa* u, const double_soa* phases, double 
   Z* xs64 = dev(reinterpret_cast<Z*>(solutions), "solutions");
   const Z* b64 = dev(reinterpret_cast<const Z*>(sources), "sources");
   if (!u64 || !ph || !xs64 || !b64) return INVERTER_FAILURE;
-  // phase A (FP32 CG-M) runs to 100 x the target: every extra decade of its
-  // recursive residual saves refinement iterations in phase B.  Measured at
-  // 32^4, m = 0.01, 4 sources x 19 shifts: 1e-5 -> 620 ms, 1e-6 -> 557 ms,
-  // 1e-7 -> 504 ms, 1e-8 -> 496 ms, 1e-9 -> 506 ms.
+  // phase A (FP32 CG-M) runs to 1000 x the target, phase B refines every
+  // system from there: a deeper phase A saves refinement iterations but
+  // carries all shifts.  Measured at 32^4, m = 0.01, 4 sources x 19 shifts,
+  // target 1e-10, factor -> ms: on a thermalised beta = 3.75 configuration
+  // 10 -> 2420, 30 -> 2375, 100 -> 2321, 300 -> 2276, 1000 -> 2234,
+  // 3000 -> 2213, 1e4 -> 2266, 3e4 -> 2366; on seeded random links
+  // 10 -> 506, 100 -> 496, 1000 -> 504, 1e4 -> 557, 1e5 -> 620.
+  // OSTAPLE_CGM_DEPTH sets the factor (between 1 and 1e6).
+  static const double depth = [] {
+    const char* e = getenv("OSTAPLE_CGM_DEPTH");
+    const double v = e ? atof(e) : 1000.0;
+    return (v >= 1.0 && v <= 1e6) ? v : 1000.0;
+  }();
   return multishift_two_phase(u64, static_cast<const double*>(ph), mass, approx->RA_b, approx->approx_order, nrhs,
-                              b64, xs64, 100.0 * res, res, max_iter, delta_frac, 1, iters_cgm, iters_refine,
+                              b64, xs64, depth * res, res, max_iter, delta_frac, 1, iters_cgm, iters_refine,
                               true_res);
 }
 
