@@ -995,8 +995,8 @@ __global__ void k_cgm_continue(cudaGraphConditionalHandle h, const CgmScal* sc, 
 // false (nothing launched, no error recorded) where the graph cannot be
 // built, and the caller runs its host-driven loop instead.
 template <typename Enq>
-bool cgm_device_loop(const Enq& enqueue_chunk, const CgmScal* sc, int* trips, int max_trips, int chunk,
-                     int* trips_out, cudaStream_t st) {
+bool cgm_device_loop(const Enq& enqueue_chunk, const CgmScal* sc, int* trips, int max_trips, int* trips_out,
+                     cudaStream_t st) {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   bool ok = cudaGraphCreate(&graph, 0) == cudaSuccess;
@@ -1035,7 +1035,6 @@ bool cgm_device_loop(const Enq& enqueue_chunk, const CgmScal* sc, int* trips, in
   OST_CUDA(cudaMemcpyAsync(trips_out, trips, sizeof(int), cudaMemcpyDeviceToHost, st));
   OST_CUDA(cudaStreamSynchronize(st));
   cudaGraphExecDestroy(exec);
-  (void)chunk;
   return true;
 }
 
@@ -1102,7 +1101,7 @@ CgmBatchResult batched_cgm_f32(const CgmBatchBuffers& B, double mass2, const dou
   int* trips = snap + 8;
   const int max_trips = max_iter / chunk + 2;
   int trips_h = 0;
-  out.device_loop = device_loop_enabled() && cgm_device_loop(enqueue_chunk, sc, trips, max_trips, chunk, &trips_h, st);
+  out.device_loop = device_loop_enabled() && cgm_device_loop(enqueue_chunk, sc, trips, max_trips, &trips_h, st);
   if (out.device_loop) {
     const int passes = trips_h < 0 ? -trips_h : trips_h;
     g_kernel_launches += (5ull * chunk + 1) * passes;
