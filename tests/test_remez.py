@@ -6,9 +6,11 @@ against the outputs of the reference's multiprecision Remez program: every
 The best relative-error approximation of a given order is unique, so the
 generator must reproduce the reference's numbers: a0, every residue and
 every shift within 1e-9 relative (the measured agreement is 3e-11 or
-better), the error within 1e-6.  Also: the reference driver's order loop,
-a .REMEZ round trip through the library's own writer and reader, the
-error bound on a dense set of points, and the rejected arguments."""
+better), the error within 1e-6.  Also: Chebyshev equioscillation of the
+error for other exponents and orders, the reference driver's order loop, a
+.REMEZ round trip through the library's own writer and reader, the error
+bound on a dense set of points, the command line and the rejected
+arguments."""
 import ctypes as C
 import json
 
@@ -98,3 +100,24 @@ def test_command_line_writes_the_reference_file_name(L, tmp_path, monkeypatch):
     back = RationalApprox()
     assert L.rationalapprox_read_custom_nomefile(C.byref(back), str(files[0]).encode()) == 0
     assert back.error <= 1e-4 and back.approx_order == 9
+
+
+@pytest.mark.parametrize("num,den,order,lmin", [(-1, 4, 12, 1e-5), (1, 8, 9, 1e-4), (-1, 2, 10, 1e-6)])
+def test_error_equioscillates(L, num, den, order, lmin):
+    """The defining property of the best approximation (Chebyshev's
+    alternation theorem): the relative error of the approximation of
+    x^|num/den| (1/r for a negative exponent) takes its extreme value E with
+    alternating signs at 2n+2 points of [lambda_min, 1]."""
+    from openstaple_gb300 import api
+    ra = api.remez(num, den, lmin, order=order)
+    xs = np.geomspace(lmin, 1.0, 200001)
+    r = np.array([L.rational_approx_evaluate(C.byref(ra), float(x)) for x in xs])
+    b = abs(num / den)
+    e = (r ** (-1.0 if num < 0 else 1.0)) / xs ** b - 1.0
+    runs, start = [], 0
+    for i in range(1, len(e) + 1):
+        if i == len(e) or np.sign(e[i]) != np.sign(e[start]):
+            runs.append(np.abs(e[start:i]).max())
+            start = i
+    assert len(runs) == 2 * order + 2
+    assert np.max(np.abs(np.array(runs) / ra.error - 1)) <= 1e-4
